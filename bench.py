@@ -1,0 +1,366 @@
+"""Benchmark: Mrays/s of the treelet-staged traversal against the plain stack
+traversal on one GB300, hits exact.
+
+Workload (one step): the 1024x1024 heightfield (2,097,152 triangles, fBm, 4
+octaves, amplitude 0.1) with 64 instanced 10K-triangle meshes (random
+rotation, translation, scale in [0.5, 2]); 1024x1024 primary rays at 2 spp
+plus one cosine-weighted bounce ray per primary ray; closest hit, opaque;
+treelets of 8 KiB.  A step traces the primary batch, then the bounce batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is the treelet-staged traversal with rays and
+hits resident in HBM; `e2e` goes through the C ABI with host buffers
+(rt_trace_host: host-to-device copy of the rays, device-to-host copy of the
+hits inside the timed region).  `--impl reference` times the CPU
+restatement of the reference's traceRay on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "treelet-prefetching-for-rt_gb300"))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+WIDTH = HEIGHT = 1024
+SPP = 2
+BUDGET = 8192
+SEED = 1
+METRIC = "Mrays/s on 1 GB300: treelet-staged vs plain traversal, hits exact; HBM GB/s"
+WORKLOAD = ("terrain 1024x1024 (2,097,152 tris, fBm 4 oct amp 0.1) + 64 instanced 10K-tri meshes; "
+            "1024x1024x2spp primary + 1 cosine bounce each (4,194,304 rays/step); closest hit, opaque; 8 KiB treelets")
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_ray():
+    """DRAM bytes per ray of the staged kernel from the committed ncu summary, if any."""
+    p = os.path.join(REPO, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(ctx_needed: bool = True):
+    import treelet_rt as rt
+
+    t0 = time.time()
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * WIDTH * HEIGHT, SEED)
+    cam = rt.default_camera(rt.SCENE_TERRAIN_INSTANCES)
+    prim = rt.camera_rays(cam, WIDTH, HEIGHT, SPP, SEED, 1e-4, 1e30)
+    return blob, prim, time.time() - t0
+
+
+def run_reference(args, rank: int, world: int) -> None:
+    """CPU restatement of the reference's traceRay on the host cores: a
+    bounded sample of the same workload per step."""
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    if rank != 0:
+        return
+    blob, prim, _ = make_workload(False)
+    bb = blob.bytes()
+    threads = os.cpu_count() or 1
+    n_prim = len(prim)
+    sample = args.ref_sample
+    idx = np.linspace(0, n_prim - 1, sample // 2).astype(np.int64)
+    ps = prim[idx]
+    ph, _, _ = orc.trace(bb, ps, 0, threads=threads)
+    bounce = rt.bounce_rays_host(blob, ps, ph, seed=SEED + 100)
+    rays = np.concatenate([ps, bounce])
+    for _ in range(args.warmup):
+        orc.trace(bb, rays[: min(len(rays), 2048)], 0, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        orc.trace(bb, rays, 0, threads=threads)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    v = len(rays) * args.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_rays_per_step": int(len(rays)), "mode": "traceRay (plain)"},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(rays)} rays per step: {len(ps)} primary rays spread over the frame + "
+                                   f"their {len(bounce)} bounce rays"},
+        "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank: int, world: int) -> None:
+    import torch
+
+    import treelet_rt as rt
+    from treelet_rt import build as rtbuild
+
+    rtbuild.build_library()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+        dist = tdist
+
+    blob, prim, t_gen = make_workload()
+    ctx = rt.Context(dev)
+    scene = rt.Scene(ctx, blob)
+    t0 = time.time()
+    tinfo = scene.form_treelets(BUDGET)
+    t_form = time.time() - t0
+    n_prim = len(prim)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    d_prim = torch.from_numpy(prim.view(np.uint8)).to(f"cuda:{dev}")
+    d_hits_p = torch.empty(n_prim * 64, dtype=torch.uint8, device=f"cuda:{dev}")
+    d_bounce = torch.empty(n_prim * 32, dtype=torch.uint8, device=f"cuda:{dev}")
+    d_hits_b = torch.empty(n_prim * 64, dtype=torch.uint8, device=f"cuda:{dev}")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    with torch.cuda.stream(stream):
+        scene.trace(d_prim, d_hits_p, rt.MODE_PLAIN, stream=sp, n=n_prim)
+        scene.bounce(d_prim, d_hits_p, d_bounce, seed=SEED + 100, stream=sp, n=n_prim)
+    stream.synchronize()
+    n_rays = 2 * n_prim
+    hit_rate = float(np.frombuffer(d_hits_p.cpu().numpy().tobytes(), rt.HIT_DTYPE)["hit_geometry"].mean())
+
+    def step(mode):
+        scene.trace(d_prim, d_hits_p, mode, stream=sp, n=n_prim)
+        scene.trace(d_bounce, d_hits_b, mode, stream=sp, n=n_prim)
+
+    def timed(mode, steps, warmup, per_batch=False):
+        for _ in range(warmup):
+            with torch.cuda.stream(stream):
+                step(mode)
+        stream.synchronize()
+        ms, ms_p, ms_b = [], [], []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                e0.record(stream)
+                scene.trace(d_prim, d_hits_p, mode, stream=sp, n=n_prim)
+                e1.record(stream)
+                scene.trace(d_bounce, d_hits_b, mode, stream=sp, n=n_prim)
+                e2.record(stream)
+            stream.synchronize()
+            ms.append(e0.elapsed_time(e2))
+            ms_p.append(e0.elapsed_time(e1))
+            ms_b.append(e1.elapsed_time(e2))
+        return ms, ms_p, ms_b
+
+    # correctness guard: staged hits must equal plain-order treelet hits
+    with torch.cuda.stream(stream):
+        scene.trace(d_prim, d_hits_p, rt.MODE_TREELET, stream=sp, n=n_prim)
+    stream.synchronize()
+    ref_hits = d_hits_p.clone()
+    with torch.cuda.stream(stream):
+        scene.trace(d_prim, d_hits_p, rt.MODE_STAGED, stream=sp, n=n_prim)
+    stream.synchronize()
+    staged_exact = bool(torch.equal(ref_hits, d_hits_p))
+
+    results = {}
+    for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET)):
+        ms, msp, msb = timed(mode, max(3, args.steps // 2), args.warmup)
+        results[name] = {"mrays_s": n_rays / (sum(ms) / len(ms)) / 1e3,
+                         "primary_mrays_s": n_prim / (sum(msp) / len(msp)) / 1e3,
+                         "bounce_mrays_s": n_prim / (sum(msb) / len(msb)) / 1e3}
+
+    # headline: staged, with clocks sampled during the timed region
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev)
+    sampler.start()
+    ms, msp, msb = timed(rt.MODE_STAGED, args.steps, args.warmup)
+    clocks = sampler.stop()
+    torch.cuda.synchronize()
+    stats = scene.stats()  # counters of the last staged launch (bounce batch)
+    with torch.cuda.stream(stream):
+        scene.trace(d_prim, d_hits_p, rt.MODE_STAGED, stream=sp, n=n_prim)
+    stream.synchronize()
+    stats_p = scene.stats()
+    total_ms = sum(ms)
+    t_local = total_ms / 1e3
+    if dist:
+        t = torch.tensor([t_local], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_local = float(t.item())
+    value = n_rays * args.steps * world / t_local / 1e6
+    results["staged"] = {"mrays_s": n_rays / (total_ms / len(ms)) / 1e3,
+                         "primary_mrays_s": n_prim / (sum(msp) / len(msp)) / 1e3,
+                         "bounce_mrays_s": n_prim / (sum(msb) / len(msb)) / 1e3}
+
+    # roofline of the dominant kernel (staged traversal), per launch (one batch)
+    peak, peak_kind = _peaks()
+    alg_p = stats_p["node_bytes"] + n_prim * (32 + 64)
+    alg_b = stats["node_bytes"] + n_prim * (32 + 64)
+    achieved = ((alg_p / (sum(msp) / len(msp)) + alg_b / (sum(msb) / len(msb))) / 2) / 1e6  # GB/s
+    traffic = _traffic_per_ray()
+    traffic_launch = None
+    if traffic and "staged_dram_bytes_per_ray" in traffic:
+        traffic_launch = int(traffic["staged_dram_bytes_per_ray"] * n_prim)
+
+    # end to end through the C ABI with host buffers (pinned)
+    h_prim = torch.from_numpy(prim.view(np.uint8)).pin_memory()
+    h_bounce = d_bounce.cpu().pin_memory()
+    h_hits = torch.empty(n_prim * 64, dtype=torch.uint8).pin_memory()
+    from treelet_rt._ffi import check, lib
+
+    def host_trace(hr):
+        check(lib().rt_trace_host(scene.handle, hr.data_ptr(), None, rt.RAY_FLAG_OPAQUE, n_prim, rt.MODE_STAGED,
+                                  h_hits.data_ptr(), None))
+
+    for _ in range(max(1, args.warmup)):
+        host_trace(h_prim)
+    e2e_t = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        host_trace(h_prim)
+        host_trace(h_bounce)
+        e2e_t.append(time.perf_counter() - t)
+    e2e = n_rays / (sum(e2e_t) / len(e2e_t)) / 1e6 * world
+
+    # CPU baseline: oracle traceRay on a bounded sample, all host threads
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import oracle as orc
+
+        threads = os.cpu_count() or 1
+        idx = np.linspace(0, n_prim - 1, args.ref_sample // 2).astype(np.int64)
+        bb = blob.bytes()
+        hb = np.frombuffer(d_bounce.cpu().numpy().tobytes(), rt.RAY_DTYPE)
+        sample = np.concatenate([prim[idx], hb[idx]])
+        t = time.perf_counter()
+        orc.trace(bb, sample, 0, threads=threads)
+        dt = time.perf_counter() - t
+        cpu = {"value": round(len(sample) / dt / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": f"{len(sample)} rays: {len(idx)} primary rays spread over the frame + their bounce rays"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / len(ms), 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "mode": "staged (treelet order, smem staging)", "l2": "flushed",
+                       "treelets": int(tinfo["n_treelets"]), "blob_bytes": int(blob.nbytes()),
+                       "primary_hit_rate": round(hit_rate, 4), "tuning": scene.get_tuning(),
+                       "setup_s": {"scene_gen": round(t_gen, 2), "treelets": round(t_form, 2)}},
+            "modes": {k: {kk: round(vv, 3) for kk, vv in v.items()} for k, v in results.items()},
+            "staged_hits_equal_treelet_order": staged_exact,
+            "staged_counters_bounce_batch": stats,
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic_launch,
+                         "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_launch": {"primary": int(alg_p), "bounce": int(alg_b)}},
+            "e2e": {"value": round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n_rays * 32,
+                    "d2h_bytes_per_step": n_rays * 64},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clocks,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    scene.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-sample", type=int, default=1000000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,306 @@
+/* treelet_rt.h - C ABI of the GB300 ray-traversal library.
+ *
+ * This is the drop-in boundary for the reference simulator's functional
+ * ray-traversal path.  In the reference, the PTX `trace_ray` op
+ * (src/cuda-sim/instructions.cc:7135-7255) calls, once per ray,
+ *
+ *   VulkanRayTracing::traceRay(...)               src/cuda-sim/vulkan_ray_tracing.h:329-341
+ *   VulkanRayTracing::traceRayWithTreelets(...)   src/cuda-sim/vulkan_ray_tracing.h:343-356
+ *
+ * which form treelets on the first call (createTreelets,
+ * src/cuda-sim/vulkan_ray_tracing.cc:823-1470), walk the BVH, store a
+ * Traversal_data record (src/cuda-sim/vulkan_rt_thread_data.h:43-58) and hand
+ * an ordered list of node memory transactions to the RT-unit timing model
+ * (thread->set_rt_transactions, vulkan_ray_tracing.cc:2252, :3040).  The
+ * timing model then looks treelets up through addrToTreeletID /
+ * treelet_roots_addr_only (vulkan_ray_tracing.cc:456-489) and makes
+ * treelet-prefetch decisions (src/gpgpu-sim/shader.cc:3419-3633).
+ *
+ * Here the same work is batched: a caller passes device arrays of rays and
+ * receives device arrays of hit records and access traces.  All functions
+ * return an rt_status; rt_last_error() gives the message of the last failure
+ * on the calling thread.  Nothing aborts and no device code traps.
+ *
+ * Addresses: a node is named by its byte offset in the scene blob divided
+ * by 64 (its "unit index"); the blob is one address space (the reference's
+ * host-to-device offsets are 0).  A treelet is named by its root's unit index,
+ * exactly as the reference names a treelet by its root address.
+ */
+#ifndef TREELET_RT_H
+#define TREELET_RT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rt_status {
+  RT_OK = 0,
+  RT_ERR_INVALID = 1,   /* bad argument */
+  RT_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+  RT_ERR_OOM = 3,       /* allocation failed */
+  RT_ERR_BLOB = 4,      /* scene blob failed validation */
+  RT_ERR_STATE = 5,     /* call order violated (e.g. trace before treelets) */
+  RT_ERR_TOO_LARGE = 6, /* size beyond a documented limit */
+  RT_ERR_TIMEOUT = 7,   /* a bounded device wait gave up */
+  RT_ERR_NO_DEVICE = 8  /* no CUDA device / kernels not loadable */
+} rt_status;
+
+/* Ray flags: SPIR-V RayFlags (SPV_KHR_ray_tracing). */
+#define RT_RAY_FLAG_OPAQUE 0x1u
+#define RT_RAY_FLAG_NO_OPAQUE 0x2u
+#define RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT 0x4u
+#define RT_RAY_FLAG_SKIP_CLOSEST_HIT 0x8u
+
+/* Traversal modes. */
+#define RT_MODE_PLAIN 0u   /* traceRay order (vulkan_ray_tracing.cc:2309-3076) */
+#define RT_MODE_TREELET 1u /* traceRayWithTreelets order (vulkan_ray_tracing.cc:1522-2307) */
+#define RT_MODE_STAGED 2u  /* treelet order; treelets staged into shared memory */
+
+/* Transaction types in a visit trace (TransactionType,
+ * src/abstract_hardware_model.h:201-211). */
+#define RT_TX_STRUCTURE 0u
+#define RT_TX_INTERNAL_NODE 1u
+#define RT_TX_INSTANCE_LEAF 2u
+#define RT_TX_LEAF_DESCRIPTOR 3u
+#define RT_TX_QUAD_LEAF 4u
+#define RT_TX_QUAD_LEAF_HIT 5u
+#define RT_TX_PROCEDURAL_LEAF 6u
+
+/* Per-ray status bits in rt_hit.status. */
+#define RT_RAY_TRACE_OVERFLOW 0x1u /* more transactions than trace capacity */
+#define RT_RAY_STACK_OVERFLOW 0x2u /* traversal stack full: result invalid */
+#define RT_RAY_HIT_PROCEDURAL 0x4u /* a procedural leaf was reached */
+#define RT_RAY_BAD_NODE 0x8u       /* a child pointer left the blob: result invalid */
+
+/* A ray: the reference's Ray {origin_tmin, dir_tmax}
+ * (src/abstract_hardware_model.h:333-370). 32 bytes. */
+typedef struct rt_ray {
+  float origin[3];
+  float tmin;
+  float dir[3];
+  float tmax;
+} rt_ray;
+
+/* Hit record: the fields of Traversal_data / Hit_data
+ * (src/cuda-sim/vulkan_rt_thread_data.h:29-58) that traversal produces,
+ * plus trace bookkeeping.  64 bytes. */
+typedef struct rt_hit {
+  uint32_t hit_geometry;     /* 1 if min_thit < Tmax */
+  uint32_t geometry_index;   /* closest leaf's GeometryIndex */
+  uint32_t primitive_index;  /* closest leaf's PrimitiveIndex0 */
+  uint32_t instance_index;   /* closest instance leaf's InstanceID */
+  float world_min_thit;
+  float barycentric[3];      /* {v, w, u} as Barycentric() returns */
+  float intersection_point[3];
+  uint32_t n_visits;         /* transactions of this ray (full count) */
+  uint32_t status;           /* RT_RAY_* bits */
+  uint32_t closest_leaf;     /* unit index of the closest quad leaf */
+  uint32_t closest_instance; /* unit index of its instance leaf */
+  uint32_t reserved;
+} rt_hit;
+
+/* Caller-owned device buffers for the access traces.  Either pointer may be
+ * NULL (that trace is not written).  Row r holds ray r's first `capacity`
+ * transactions in order.
+ *   visits[r * capacity + j]   = unit_index << 3 | transaction type
+ *   treelets[r * capacity + j] = treelet root unit index of that transaction
+ *                                (the reference's "RayID,<ids>" line,
+ *                                vulkan_ray_tracing.cc:2256-2262) */
+typedef struct rt_trace_buf {
+  uint32_t* visits;
+  uint32_t* treelets;
+  uint32_t capacity;
+} rt_trace_buf;
+
+typedef struct rt_blob rt_blob;   /* host scene blob */
+typedef struct rt_ctx rt_ctx;     /* device context */
+typedef struct rt_scene rt_scene; /* device-resident scene */
+
+/* ---------------- errors ---------------- */
+const char* rt_last_error(void);
+const char* rt_version(void);
+
+/* ---------------- host scene blobs ---------------- */
+
+/* Synthetic scene kinds (seeded).  See rt_gen_scene. */
+#define RT_SCENE_CUBE_PLANE 0u        /* n random small triangles in the unit cube + 2-triangle ground plane */
+#define RT_SCENE_TERRAIN_INSTANCES 1u /* heightfield (n triangles) + 64 instanced 10K-triangle meshes */
+#define RT_SCENE_BLOBS 2u             /* n small triangles in 16 Gaussian blobs (sigma 0.05) */
+#define RT_SCENE_CUBE 3u              /* n random small triangles in the unit cube */
+#define RT_SCENE_SHARED_BLAS 4u       /* one n-triangle mesh instanced 4 times (shared BLAS) */
+
+rt_status rt_gen_scene(uint32_t kind, uint64_t n_tris, uint64_t seed, rt_blob** out);
+
+/* Builds a blob from caller meshes and instances.  tris holds 9 floats per
+ * triangle; mesh m owns triangles [mesh_first[m], mesh_first[m+1]).  Each
+ * instance i references mesh inst_mesh[i] with object-to-world transform
+ * inst_o2w[12*i .. 12*i+11] (row-vector convention: rows 0-2 linear part,
+ * row 3 translation) and InstanceID inst_id[i]. */
+rt_status rt_blob_build(const float* tris, const uint32_t* mesh_first, uint32_t n_meshes,
+                        const uint32_t* inst_mesh, const float* inst_o2w, const uint32_t* inst_id,
+                        uint32_t n_instances, rt_blob** out);
+
+/* Wraps existing bytes (copied) in the reference layout. */
+rt_status rt_blob_wrap(const void* bytes, uint64_t n_bytes, rt_blob** out);
+rt_status rt_blob_data(const rt_blob* blob, const uint8_t** bytes, uint64_t* n_bytes);
+void rt_blob_free(rt_blob* blob);
+
+/* Pinhole camera rays on the host: W x H pixels, spp samples each,
+ * pixel-centre samples when jitter_seed == 0, else jittered.  Rays are
+ * ordered sample-major, then 8x4 pixel tiles (one warp per tile, the
+ * launch tiling of vkCmdTraceRaysKHR, vulkan_ray_tracing.cc:3503-3588). */
+typedef struct rt_camera {
+  float eye[3];
+  float target[3];
+  float up[3];
+  float vfov_deg;
+} rt_camera;
+rt_status rt_scene_default_camera(uint32_t kind, rt_camera* cam);
+rt_status rt_gen_camera_rays(const rt_camera* cam, uint32_t width, uint32_t height, uint32_t spp,
+                             uint64_t jitter_seed, float tmin, float tmax, rt_ray* out);
+
+/* Cosine-weighted bounce rays about the geometric normal at each hit (host).
+ * Rays whose hit_geometry is 0 get an empty interval (tmin = 1, tmax = 0). */
+rt_status rt_gen_bounce_rays_host(const rt_blob* blob, const rt_ray* rays, const rt_hit* hits, uint64_t n,
+                                  uint64_t seed, float tmin, float tmax, rt_ray* out);
+
+/* Validates a blob: header, child pointers in range, child sizes/types legal.
+ * Returns RT_ERR_BLOB with a message on the first problem. */
+rt_status rt_blob_validate(const rt_blob* blob);
+
+/* ---------------- device context and scenes ---------------- */
+rt_status rt_ctx_create(int device, rt_ctx** out);
+rt_status rt_ctx_destroy(rt_ctx* ctx);
+
+/* Uploads a blob (validated first). */
+rt_status rt_scene_create(rt_ctx* ctx, const rt_blob* blob, rt_scene** out);
+rt_status rt_scene_destroy(rt_scene* scene);
+/* Device pointer and size of the uploaded blob. */
+rt_status rt_scene_device_blob(const rt_scene* scene, const void** dptr, uint64_t* n_bytes);
+
+/* ---------------- treelets ---------------- */
+
+/* Treelet partition of the scene with a byte budget per treelet
+ * (createTreelets, vulkan_ray_tracing.cc:823-1470, with the node -> treelet
+ * map of buildNodeToRootMap, :475-489).  Must precede RT_MODE_TREELET /
+ * RT_MODE_STAGED traces.  Re-forming replaces the previous partition. */
+typedef struct rt_treelet_info {
+  uint32_t n_treelets;
+  uint32_t max_treelet_bytes;
+  uint64_t member_entries;  /* sum of member-list lengths after de-dup */
+  uint64_t image_bytes;     /* bytes of all staged treelet images */
+  uint32_t largest_image;   /* bytes of the largest treelet image */
+  uint32_t reserved;
+} rt_treelet_info;
+rt_status rt_treelets_form(rt_scene* scene, uint32_t max_treelet_bytes, rt_treelet_info* info);
+
+/* Host copies of the partition:
+ *   roots[k]        root unit index of treelet k (k ascending root address =
+ *                   treelet_addr_to_metadata_idx order, vulkan_ray_tracing.cc:1310-1334)
+ *   member_first[k] start of treelet k's members in `members`, k = 0..n (n+1 entries)
+ *   members[...]    member unit indices in formation order, de-duplicated
+ *   member_bytes[..] size charged for each member (64 / 128)
+ *   node_root[u]    treelet root of unit u (addrToTreeletID) or 0xFFFFFFFF
+ * Any pointer may be NULL.  Sizes: n_treelets, n_treelets + 1,
+ * member_entries, member_entries, blob bytes / 64. */
+rt_status rt_treelets_get(const rt_scene* scene, uint32_t* roots, uint64_t* member_first, uint32_t* members,
+                          uint16_t* member_bytes, uint32_t* node_root);
+
+/* Treelet-contiguous relayout (remapBVHToTreeletLayout,
+ * vulkan_ray_tracing.cc:1473-1509): new_addr[u] for every unit, or
+ * 0xFFFFFFFFFFFFFFFF for units not placed; treelet k starts at
+ * k * (max_treelet_bytes + stride).  Returns RT_ERR_STATE where the reference
+ * asserts (a treelet root already placed inside an earlier treelet). */
+rt_status rt_treelets_remap(const rt_scene* scene, uint32_t stride, uint64_t* new_addr);
+
+/* ---------------- tracing ---------------- */
+
+/* Traces n rays.  All array arguments are device pointers on the scene's
+ * device; `flags` may be NULL (every ray uses default_flags).  `trace` may be
+ * NULL.  Stream-ordered on `stream` (a cudaStream_t, NULL = default stream). */
+rt_status rt_trace(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t n,
+                   uint32_t mode, rt_hit* hits, const rt_trace_buf* trace, void* stream);
+
+/* The same with host arrays: copies rays in and hits (and traces, whose
+ * pointers are then host pointers) out; synchronous. */
+rt_status rt_trace_host(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
+                        uint32_t n, uint32_t mode, rt_hit* hits, const rt_trace_buf* trace);
+
+/* Traversal tuning: stack entries per ray, threads per block, rays per
+ * staging epoch.  0 keeps the current value. */
+typedef struct rt_tuning {
+  uint32_t block_threads;   /* threads per CTA for RT_MODE_PLAIN / RT_MODE_TREELET */
+  uint32_t staged_threads;  /* threads per CTA for RT_MODE_STAGED */
+  uint32_t staged_epoch;    /* nodes a ray processes between staging decisions */
+  uint32_t staged_slots;    /* treelets resident in shared memory at once */
+} rt_tuning;
+rt_status rt_scene_set_tuning(rt_scene* scene, const rt_tuning* t);
+rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);
+
+/* Counters of the last rt_trace on this scene (read after the stream is
+ * synchronised): node bytes read by the walk, bytes copied into shared memory
+ * by treelet staging, node reads served from shared memory / global memory. */
+typedef struct rt_trace_stats {
+  uint64_t node_bytes;
+  uint64_t staged_bytes;
+  uint64_t smem_reads;
+  uint64_t gmem_reads;
+  uint64_t stagings;
+  uint64_t device_status; /* nonzero: a bounded wait gave up (staging was switched off) */
+} rt_trace_stats;
+rt_status rt_trace_stats_get(rt_scene* scene, rt_trace_stats* out);
+
+/* Device version of rt_gen_bounce_rays_host (stream-ordered). */
+rt_status rt_gen_bounce_rays(rt_scene* scene, const rt_ray* rays, const rt_hit* hits, uint32_t n, uint64_t seed,
+                             float tmin, float tmax, rt_ray* out, void* stream);
+
+/* ---------------- treelet-prefetch decision ---------------- */
+
+/* Heuristics of -treelet_prefetch_heuristic (src/gpgpu-sim/gpu-sim.cc:389-466). */
+#define RT_PREFETCH_ALWAYS 0u      /* most popular treelet, always */
+#define RT_PREFETCH_POPULARITY 1u  /* only if its share >= threshold */
+#define RT_PREFETCH_PARTIAL 2u     /* round(share * nodes) nodes from the start */
+#define RT_PREFETCH_LATTER 3u      /* the same count from the end */
+#define RT_NO_TREELET 0xFFFFFFFFu
+
+typedef struct rt_prefetch_params {
+  uint32_t heuristic;       /* RT_PREFETCH_* */
+  uint32_t max_queue;       /* -max_prefetch_queue_size */
+  double threshold;         /* -treelet_prefetch_threshold */
+  uint32_t second_prefetch; /* -prefetch_next_treelet_when_queue_empty */
+  uint32_t reserved;
+} rt_prefetch_params;
+
+/* Per-RT-unit state carried from one decision to the next. */
+typedef struct rt_prefetch_state {
+  uint32_t last_prefetched;        /* root unit or RT_NO_TREELET */
+  uint32_t last_prefetched_second; /* root unit or RT_NO_TREELET */
+  uint32_t last_rejected;          /* root unit or RT_NO_TREELET */
+  uint32_t queue_len;              /* 32 B requests waiting in the unit's prefetch queue */
+} rt_prefetch_state;
+
+typedef struct rt_prefetch_decision {
+  uint32_t treelet;        /* most popular treelet root, or RT_NO_TREELET */
+  uint32_t count;          /* lanes whose next access is in it */
+  uint32_t total;          /* lanes with a next access */
+  uint32_t submitted;      /* 1 if its nodes were queued */
+  uint32_t first_member;   /* queued members: [first_member, first_member + n_members) */
+  uint32_t n_members;      /*   of the treelet's member list (rt_treelets_get order) */
+  uint32_t chunks;         /* 32 B requests queued */
+  uint32_t second_treelet; /* treelet queued by the second-prefetch rule, or RT_NO_TREELET */
+} rt_prefetch_decision;
+
+/* One decision per RT unit (shader.cc:3419-3683): n_units groups of `lanes`
+ * next-access unit indices (RT_NO_TREELET = lane idle).  Device arrays;
+ * state is read and updated in place.  Needs rt_treelets_form. */
+rt_status rt_prefetch_decide(rt_scene* scene, const uint32_t* next_unit, uint32_t n_units, uint32_t lanes,
+                             const rt_prefetch_params* params, rt_prefetch_state* state, rt_prefetch_decision* out,
+                             void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TREELET_RT_H */

@@ -1,0 +1,144 @@
+"""ctypes wrapper of liboracle_rt.so: the CPU restatement of the reference's
+traversal, treelet partition and prefetch decision.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
+baseline of bench.py use it, as the checker.  See oracle_rt.h for the parity
+status (decoders pinned against the reference's header; traversal, treelets
+and prefetch decision unpinned: no reference tests or golden vectors exist).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle_rt.so")
+
+RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("hit_geometry", "<u4"), ("geometry_index", "<u4"), ("primitive_index", "<u4"),
+                      ("instance_index", "<u4"), ("world_min_thit", "<f4"), ("barycentric", "<f4", 3),
+                      ("intersection_point", "<f4", 3), ("n_visits", "<u4"), ("status", "<u4"),
+                      ("closest_leaf", "<u4"), ("closest_instance", "<u4"), ("reserved", "<u4")])
+STATE_DTYPE = np.dtype([("last_prefetched", "<u4"), ("last_prefetched_second", "<u4"), ("last_rejected", "<u4"),
+                        ("queue_len", "<u4")])
+DECISION_DTYPE = np.dtype([("treelet", "<u4"), ("count", "<u4"), ("total", "<u4"), ("submitted", "<u4"),
+                           ("first_member", "<u4"), ("n_members", "<u4"), ("chunks", "<u4"),
+                           ("second_treelet", "<u4")])
+
+
+class _Params(C.Structure):
+    _fields_ = [("heuristic", C.c_uint32), ("max_queue", C.c_uint32), ("threshold", C.c_double),
+                ("second_prefetch", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle_rt.cpp")
+    deps = [src, os.path.join(HERE, "oracle_rt.h"), os.path.join(os.path.dirname(HERE), "include", "treelet_rt.h")]
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
+        subprocess.run(["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-shared", "-o", LIB, src,
+                        "-lpthread"], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp = C.c_void_p
+        L.oracle_form_treelets.restype = vp
+        L.oracle_form_treelets.argtypes = [vp, C.c_uint64, C.c_int]
+        L.oracle_treelets_free.argtypes = [vp]
+        L.oracle_last_error.restype = C.c_char_p
+        L.oracle_treelets_sizes.argtypes = [vp, vp, vp]
+        L.oracle_treelets_get.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, vp]
+        L.oracle_remap.restype = C.c_int
+        L.oracle_remap.argtypes = [vp, C.c_int, C.c_uint32, C.c_uint64, vp]
+        L.oracle_trace.restype = C.c_int
+        L.oracle_trace.argtypes = [vp, C.c_uint64, vp, vp, vp, C.c_uint32, C.c_uint64, C.c_int, vp, vp, vp,
+                                   C.c_uint32, C.c_int]
+        L.oracle_prefetch_decide.restype = C.c_int
+        L.oracle_prefetch_decide.argtypes = [vp, vp, C.c_uint32, C.POINTER(_Params), vp, vp]
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class Treelets:
+    def __init__(self, blob: np.ndarray, max_bytes: int):
+        self.blob = np.ascontiguousarray(blob, np.uint8)
+        self.max_bytes = max_bytes
+        h = lib().oracle_form_treelets(self.blob.ctypes.data, self.blob.nbytes, max_bytes)
+        if not h:
+            raise OracleError(lib().oracle_last_error().decode())
+        self.h = C.c_void_p(h)
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().oracle_treelets_free(self.h)
+        except Exception:
+            pass
+
+    def get(self) -> dict:
+        n = C.c_uint32()
+        m = C.c_uint64()
+        lib().oracle_treelets_sizes(self.h, C.byref(n), C.byref(m))
+        n_units = self.blob.nbytes // 64
+        roots = np.zeros(n.value, np.uint32)
+        first = np.zeros(n.value + 1, np.uint64)
+        members = np.zeros(m.value, np.uint32)
+        mbytes = np.zeros(m.value, np.uint16)
+        node_root = np.zeros(n_units, np.uint32)
+        lib().oracle_treelets_get(self.h, n_units, roots.ctypes.data, first.ctypes.data, members.ctypes.data,
+                                  mbytes.ctypes.data, node_root.ctypes.data)
+        return dict(roots=roots, member_first=first, members=members, member_bytes=mbytes, node_root=node_root)
+
+    def remap(self, stride: int = 0) -> np.ndarray:
+        n_units = self.blob.nbytes // 64
+        out = np.zeros(n_units, np.uint64)
+        if lib().oracle_remap(self.h, self.max_bytes, stride, n_units, out.ctypes.data) != 0:
+            raise OracleError(lib().oracle_last_error().decode())
+        return out
+
+
+def trace(blob: np.ndarray, rays: np.ndarray, mode: int = 0, treelets: Treelets | None = None, flags=None,
+          default_flags: int = 1, capacity: int = 0, want_visits: bool = False, want_treelets: bool = False,
+          threads: int = 1):
+    """mode 0 = traceRay, 1 = traceRayWithTreelets.  Returns (hits, visits, treelet ids)."""
+    blob = np.ascontiguousarray(blob, np.uint8)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE)
+    vis = np.zeros((n, capacity), np.uint32) if want_visits else None
+    tl = np.zeros((n, capacity), np.uint32) if want_treelets else None
+    fl = None if flags is None else np.ascontiguousarray(flags, np.uint32)
+    rc = lib().oracle_trace(blob.ctypes.data, blob.nbytes, treelets.h if treelets else None, rays.ctypes.data,
+                            fl.ctypes.data if fl is not None else None, default_flags, n, mode, hits.ctypes.data,
+                            vis.ctypes.data if vis is not None else None, tl.ctypes.data if tl is not None else None,
+                            capacity, threads)
+    if rc != 0:
+        raise OracleError(lib().oracle_last_error().decode())
+    return hits, vis, tl
+
+
+def prefetch_decide(treelets: Treelets, next_unit: np.ndarray, heuristic: int = 0, max_queue: int = 1000000,
+                    threshold: float = 0.5, second_prefetch: bool = False, state: np.ndarray | None = None):
+    """One RT unit's decision.  Returns (decision, new state) as structured scalars."""
+    nu = np.ascontiguousarray(next_unit, np.uint32)
+    st = np.zeros(1, STATE_DTYPE) if state is None else np.array(state, STATE_DTYPE).reshape(1).copy()
+    if state is None:
+        st["last_prefetched"] = st["last_prefetched_second"] = st["last_rejected"] = 0xFFFFFFFF
+    out = np.zeros(1, DECISION_DTYPE)
+    p = _Params(heuristic, max_queue, threshold, int(second_prefetch), 0)
+    lib().oracle_prefetch_decide(treelets.h, nu.ctypes.data, len(nu), C.byref(p), st.ctypes.data, out.ctypes.data)
+    return out[0], st[0]

@@ -1,0 +1,60 @@
+/* oracle_rt.h - CPU restatement of the reference's functional ray-traversal
+ * path.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and the
+ * CPU-baseline leg of the benchmark call it as the checker; the library never
+ * links or calls it.
+ *
+ * Parity status: the reference (Vulkan-Sim's vulkan_ray_tracing.cc) cannot be
+ * compiled here (it needs Mesa, the Vulkan SDK, Boost, flex and bison), and it
+ * ships no tests or golden vectors for this path.  The node decoders,
+ * set_child_bounds and float4x4 product are pinned against the reference's own
+ * header compiled with a stub (oracle/ref_pin/); the traversal, treelet
+ * partition and prefetch decision are restated line by line and checked
+ * against hand-derived known answers only: parity unpinned for those parts.
+ */
+#ifndef ORACLE_RT_H
+#define ORACLE_RT_H
+#include <stdint.h>
+
+#include "../include/treelet_rt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_treelets oracle_treelets;
+
+/* createTreelets + buildNodeToRootMap over a blob (vulkan_ray_tracing.cc:823-1470,
+ * :475-489).  Returns NULL on a condition where the reference asserts; the
+ * message is in oracle_last_error(). */
+oracle_treelets* oracle_form_treelets(const uint8_t* blob, uint64_t n_bytes, int max_bytes);
+void oracle_treelets_free(oracle_treelets* t);
+const char* oracle_last_error(void);
+
+/* Sizes: *n_treelets and *n_members. */
+void oracle_treelets_sizes(const oracle_treelets* t, uint32_t* n_treelets, uint64_t* n_members);
+/* Same layout as rt_treelets_get (any pointer may be NULL). */
+void oracle_treelets_get(const oracle_treelets* t, uint64_t n_units, uint32_t* roots, uint64_t* member_first,
+                         uint32_t* members, uint16_t* member_bytes, uint32_t* node_root);
+/* remapBVHToTreeletLayout (:1473-1509).  Returns 0, or -1 where the reference asserts. */
+int oracle_remap(const oracle_treelets* t, int max_bytes, uint32_t stride, uint64_t n_units, uint64_t* new_addr);
+
+/* Traces n rays with traceRay (mode 0, :2309-3076) or traceRayWithTreelets
+ * (mode 1, :1522-2307).  `tl` is required for mode 1 and for treelet traces.
+ * visits / treelets / capacity follow rt_trace_buf.  threads <= 1 runs on the
+ * calling thread, otherwise contiguous ray ranges per std::thread.
+ * Returns 0 or -1 (message in oracle_last_error). */
+int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* tl, const rt_ray* rays,
+                 const uint32_t* flags, uint32_t default_flags, uint64_t n, int mode, rt_hit* hits, uint32_t* visits,
+                 uint32_t* treelets, uint32_t capacity, int threads);
+
+/* Treelet-prefetch decision of one RT unit (shader.cc:3419-3633 and the
+ * second-treelet step :3645-3683).  next_unit holds each resident lane's next
+ * access (unit index) or 0xFFFFFFFF.  State and decision use the library's
+ * structs (treelet_rt.h). */
+int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
+                           const rt_prefetch_params* p, rt_prefetch_state* state, rt_prefetch_decision* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,157 @@
+"""GPU traversal vs the CPU oracle: hit records, node-visit traces and
+treelet-access traces must be bit-identical (the kernels keep the reference's
+FP32 operation order with FMA contraction off, so hit t is compared bit for
+bit, no tolerance)."""
+import numpy as np
+import pytest
+
+from helpers import assert_hits_equal, assert_traces_equal, edge_rays
+
+pytestmark = pytest.mark.gpu
+
+CAP = 512
+
+
+def _modes():
+    import treelet_rt as rt
+
+    return [(rt.MODE_PLAIN, 0, "plain"), (rt.MODE_TREELET, 1, "treelet"), (rt.MODE_STAGED, 1, "staged")]
+
+
+def _check_all_modes(ctx, blob, rays, budget=8192, flags=None, default_flags=1, cap=CAP, tuning=None):
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(budget)
+    if tuning:
+        scene.set_tuning(**tuning)
+    tl = orc.Treelets(blob.bytes(), budget)
+    for mode, omode, name in _modes():
+        hits, vis, tids = scene.trace_host(rays, mode, flags=flags, default_flags=default_flags, capacity=cap,
+                                           want_visits=True, want_treelets=True)
+        oh, ov, ot = orc.trace(blob.bytes(), rays, omode, tl, flags=flags, default_flags=default_flags, capacity=cap,
+                               want_visits=True, want_treelets=True, threads=8)
+        assert not (oh["status"] & (rt.RAY_STACK_OVERFLOW | rt.RAY_BAD_NODE)).any()
+        assert_hits_equal(hits, oh, f"{name} hits")
+        assert_traces_equal(vis, ov, oh["n_visits"], f"{name} visits")
+        assert_traces_equal(tids, ot, oh["n_visits"], f"{name} treelet ids")
+    scene.close()
+    return oh
+
+
+def test_cube_plane_primary(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 16384, 1)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 128, 128, 1, 0, 1e-4, 1e30)
+    oh = _check_all_modes(ctx, blob, rays)
+    assert oh["hit_geometry"].mean() > 0.3
+
+
+def test_cube_plane_bounce(ctx):
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 16384, 2)
+    prim = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 96, 96, 1, 5, 1e-4, 1e30)
+    ph, _, _ = orc.trace(blob.bytes(), prim, 0)
+    bounce = rt.bounce_rays_host(blob, prim, ph, seed=11)
+    _check_all_modes(ctx, blob, bounce)
+
+
+def test_shared_blas_instances(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_SHARED_BLAS, 512, 4)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_SHARED_BLAS), 64, 64, 2, 9, 1e-4, 1e30)
+    for budget in (512, 2048, 8192):
+        _check_all_modes(ctx, blob, rays, budget=budget)
+
+
+def test_terrain_instances_small(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 64 * 64, 5)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_TERRAIN_INSTANCES), 64, 64, 1, 3, 1e-4, 1e30)
+    oh = _check_all_modes(ctx, blob, rays)
+    assert oh["hit_geometry"].mean() > 0.9
+
+
+@pytest.mark.parametrize("budget", [4096, 8192, 16384, 32768])
+def test_budget_sweep_ao(ctx, budget):
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    blob = rt.Blob.gen(rt.SCENE_BLOBS, 60000, 6)
+    prim = rt.camera_rays(rt.default_camera(rt.SCENE_BLOBS), 48, 48, 1, 0, 1e-4, 1e30)
+    ph, _, _ = orc.trace(blob.bytes(), prim, 0)
+    hit = ph["hit_geometry"] == 1
+    ao = rt.bounce_rays_host(blob, prim[hit], ph[hit], seed=21, tmin=1e-4, tmax=0.1)
+    ao = np.repeat(ao, 2)
+    _check_all_modes(ctx, blob, ao, budget=budget, default_flags=rt.RAY_FLAG_TERMINATE_ON_FIRST_HIT | rt.RAY_FLAG_OPAQUE)
+
+
+def test_non_opaque_and_mixed_flags(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 4096, 7)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 40, 40, 1, 0, 1e-4, 1e30)
+    rng = np.random.default_rng(3)
+    flags = rng.choice(np.array([0, 1, 4, 5, 8, 9, 2], np.uint32), size=len(rays))
+    _check_all_modes(ctx, blob, rays, flags=flags)
+    _check_all_modes(ctx, blob, rays, default_flags=0)
+
+
+def test_edge_rays(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 2048, 8)
+    _check_all_modes(ctx, blob, edge_rays())
+
+
+def test_trace_overflow_truncates(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 4096, 9)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 32, 32, 1, 0, 1e-4, 1e30)
+    oh = _check_all_modes(ctx, blob, rays, cap=6)
+    assert (oh["status"] & rt.RAY_TRACE_OVERFLOW).any()
+
+
+@pytest.mark.parametrize("tuning", [dict(staged_slots=1, staged_epoch=1), dict(staged_slots=8, staged_epoch=4),
+                                    dict(staged_slots=16, staged_epoch=64, staged_threads=128),
+                                    dict(block_threads=64, staged_threads=64)])
+def test_staged_tuning_invariance(ctx, tuning):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 16384, 10)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 64, 64, 1, 1, 1e-4, 1e30)
+    _check_all_modes(ctx, blob, rays, tuning=tuning)
+
+
+def test_empty_batch(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 1024, 1)
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    for mode, _, _ in _modes():
+        hits, _, _ = scene.trace_host(np.zeros(0, rt.RAY_DTYPE), mode)
+        assert len(hits) == 0
+    scene.close()
+
+
+def test_staged_serves_from_shared_memory(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 16384, 1)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 128, 128, 1, 0, 1e-4, 1e30)
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    scene.trace_host(rays, rt.MODE_STAGED)
+    st = scene.stats()
+    assert st["device_status"] == 0
+    assert st["stagings"] > 0 and st["staged_bytes"] > 0
+    assert st["smem_reads"] > 0
+    scene.close()

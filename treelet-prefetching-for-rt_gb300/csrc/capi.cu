@@ -1,0 +1,532 @@
+// C ABI: contexts, device scenes, treelets, tracing, bounce rays and the
+// prefetch decision.  Every entry point returns an rt_status and records a
+// message for rt_last_error(); none aborts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "capi_internal.h"
+#include "trace_kernels.cuh"
+#include "prefetch_kernels.cuh"
+#include "trace_treelet.cuh"
+#include "treelets.h"
+
+namespace rti {
+
+namespace {
+thread_local std::string g_error;
+}
+
+void set_error(const std::string& msg) { g_error = msg; }
+rt_status fail(rt_status s, const std::string& msg) {
+  g_error = msg;
+  return s;
+}
+
+bool validate_blob(const uint8_t* b, uint64_t n, std::string* err) {
+  auto bad = [&](const std::string& m) {
+    if (err) *err = m;
+    return false;
+  };
+  if (!b || n < 128 || n % 64) return bad("blob must be at least 128 bytes and a multiple of 64");
+  const uint64_t units = n / 64;
+  if (units >= (1ull << 29)) return bad("blob larger than 32 GiB");
+  auto rd64 = [&](uint64_t off) {
+    uint64_t v;
+    std::memcpy(&v, b + off, 8);
+    return v;
+  };
+  std::vector<uint8_t> seen(units, 0);
+  struct Item {
+    uint64_t unit;
+    bool top;
+  };
+  std::vector<Item> work;
+  const uint64_t root = rd64(rtf::HDR_ROOT_OFFSET);
+  if (root % 64 || root / 64 >= units || root == 0) return bad("TLAS RootNodeOffset out of range");
+  work.push_back({root / 64, true});
+  while (!work.empty()) {
+    const Item it = work.back();
+    work.pop_back();
+    if (seen[it.unit]) continue;
+    seen[it.unit] = 1;
+    const uint8_t* p = b + it.unit * 64;
+    int32_t child_off;
+    std::memcpy(&child_off, p + rtf::IN_CHILD_OFFSET, 4);
+    bool any = false;
+    for (int i = 0; i < 6; ++i) any |= (p[rtf::IN_CHILD_INFO + i] & 3u) != 0;
+    if (!any) continue;
+    if (child_off <= 0) return bad("internal node with a child block that does not follow it");
+    uint64_t c = it.unit + (uint64_t)child_off;
+    for (int i = 0; i < 6; ++i) {
+      const uint8_t info = p[rtf::IN_CHILD_INFO + i];
+      const uint32_t sz = rtf::child_size_units(info), ty = rtf::child_type(info);
+      if (sz) {
+        if (c + sz > units) return bad("child outside the blob");
+        if (ty == rtf::CT_INTERNAL) {
+          work.push_back({c, it.top});
+        } else if (it.top) {
+          if (ty != rtf::CT_INSTANCE || sz != 2) return bad("top-level leaf that is not a 128-byte instance leaf");
+          if (!seen[c]) {
+            seen[c] = 1;
+            const uint64_t hdr = c * 64 + rd64(c * 64 + rtf::IL_BVH_ADDRESS);
+            if (hdr % 64 || hdr / 64 >= units) return bad("instance BVHAddress out of range");
+            const uint64_t broot = hdr + rd64(hdr + rtf::HDR_ROOT_OFFSET);
+            if (broot % 64 || broot / 64 >= units || broot <= hdr) return bad("BLAS RootNodeOffset out of range");
+            work.push_back({broot / 64, false});
+          }
+        } else {
+          if (ty != rtf::CT_QUAD && ty != rtf::CT_PROCEDURAL) return bad("bottom-level leaf of unknown type");
+        }
+      }
+      c += sz;
+    }
+  }
+  return true;
+}
+
+}  // namespace rti
+
+struct rt_ctx {
+  int device = 0;
+};
+
+struct rt_scene {
+  rt_ctx* ctx = nullptr;
+  std::vector<uint8_t> host_blob;
+  uint8_t* d_blob = nullptr;
+  uint64_t blob_bytes = 0;
+  uint32_t n_units = 0;
+  // treelets
+  bool has_treelets = false;
+  rtt::Partition part;
+  uint2* d_meta = nullptr;
+  uint8_t* d_images = nullptr;
+  unsigned long long* d_image_off = nullptr;
+  uint32_t* d_roots = nullptr;
+  unsigned long long* d_member_first = nullptr;
+  uint16_t* d_member_bytes = nullptr;
+  uint32_t slot_bytes = 0;
+  // per-launch counters and status (library scratch)
+  unsigned long long* d_stats = nullptr;
+  uint32_t* d_status = nullptr;
+  rt_tuning tuning{128, 256, 16, 4};
+  // host-buffer path scratch
+  cudaStream_t stream = nullptr;
+  void* d_io = nullptr;
+  size_t io_bytes = 0;
+};
+
+namespace {
+
+constexpr int kPlainCap = 96;
+constexpr int kTreeletCap = 96;
+
+rt_status cuda_fail(cudaError_t e, const char* what) {
+  return rti::fail(RT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define RT_CUDA(call)                                    \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+  } while (0)
+
+template <class T>
+rt_status dalloc(T** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) return rti::fail(RT_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return RT_OK;
+}
+
+void free_treelets(rt_scene* s) {
+  cudaFree(s->d_meta);
+  cudaFree(s->d_images);
+  cudaFree(s->d_image_off);
+  cudaFree(s->d_roots);
+  cudaFree(s->d_member_first);
+  cudaFree(s->d_member_bytes);
+  s->d_meta = nullptr;
+  s->d_images = nullptr;
+  s->d_image_off = nullptr;
+  s->d_roots = nullptr;
+  s->d_member_first = nullptr;
+  s->d_member_bytes = nullptr;
+  s->has_treelets = false;
+}
+
+int max_smem_per_block() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rt_last_error(void) { return rti::g_error.c_str(); }
+const char* rt_version(void) { return "treelet_rt 0.1 (sm_103a)"; }
+
+rt_status rt_blob_validate(const rt_blob* blob) {
+  if (!blob) return rti::fail(RT_ERR_INVALID, "rt_blob_validate: NULL");
+  std::string err;
+  if (!rti::validate_blob(blob->bytes.data(), blob->bytes.size(), &err)) return rti::fail(RT_ERR_BLOB, err);
+  return RT_OK;
+}
+
+rt_status rt_ctx_create(int device, rt_ctx** out) {
+  if (!out) return rti::fail(RT_ERR_INVALID, "rt_ctx_create: out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return rti::fail(RT_ERR_NO_DEVICE, "rt_ctx_create: no CUDA device");
+  if (device < 0 || device >= n) return rti::fail(RT_ERR_INVALID, "rt_ctx_create: bad device ordinal");
+  RT_CUDA(cudaSetDevice(device));
+  auto* c = new rt_ctx();
+  c->device = device;
+  *out = c;
+  return RT_OK;
+}
+
+rt_status rt_ctx_destroy(rt_ctx* ctx) {
+  delete ctx;
+  return RT_OK;
+}
+
+rt_status rt_scene_create(rt_ctx* ctx, const rt_blob* blob, rt_scene** out) {
+  if (!ctx || !blob || !out) return rti::fail(RT_ERR_INVALID, "rt_scene_create: NULL argument");
+  *out = nullptr;
+  std::string err;
+  if (!rti::validate_blob(blob->bytes.data(), blob->bytes.size(), &err)) return rti::fail(RT_ERR_BLOB, err);
+  RT_CUDA(cudaSetDevice(ctx->device));
+  auto* s = new rt_scene();
+  s->ctx = ctx;
+  s->host_blob = blob->bytes;
+  s->blob_bytes = blob->bytes.size();
+  s->n_units = (uint32_t)(s->blob_bytes / 64);
+  rt_status st = dalloc(&s->d_blob, s->blob_bytes);
+  if (st == RT_OK) st = dalloc(&s->d_stats, sizeof(unsigned long long) * rtk::ST_COUNT);
+  if (st == RT_OK) st = dalloc(&s->d_status, sizeof(uint32_t));
+  if (st != RT_OK) {
+    rt_scene_destroy(s);
+    return st;
+  }
+  cudaError_t e = cudaMemcpy(s->d_blob, blob->bytes.data(), s->blob_bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT);
+  if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    rt_scene_destroy(s);
+    return cuda_fail(e, "rt_scene_create");
+  }
+  *out = s;
+  return RT_OK;
+}
+
+rt_status rt_scene_destroy(rt_scene* s) {
+  if (!s) return RT_OK;
+  cudaSetDevice(s->ctx->device);
+  free_treelets(s);
+  cudaFree(s->d_blob);
+  cudaFree(s->d_stats);
+  cudaFree(s->d_status);
+  cudaFree(s->d_io);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return RT_OK;
+}
+
+rt_status rt_scene_device_blob(const rt_scene* s, const void** dptr, uint64_t* n_bytes) {
+  if (!s || !dptr || !n_bytes) return rti::fail(RT_ERR_INVALID, "rt_scene_device_blob: NULL");
+  *dptr = s->d_blob;
+  *n_bytes = s->blob_bytes;
+  return RT_OK;
+}
+
+rt_status rt_treelets_form(rt_scene* s, uint32_t max_treelet_bytes, rt_treelet_info* info) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_treelets_form: NULL scene");
+  std::string err;
+  rtt::Partition p;
+  if (!rtt::form_treelets(s->host_blob.data(), s->blob_bytes, max_treelet_bytes, p, &err))
+    return rti::fail(RT_ERR_INVALID, "rt_treelets_form: " + err);
+  std::vector<uint8_t> store;
+  rtt::build_images(s->host_blob.data(), p, store);
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  free_treelets(s);
+  const uint32_t n = (uint32_t)p.roots.size();
+  std::vector<uint2> meta(s->n_units);
+  for (uint32_t u = 0; u < s->n_units; ++u) meta[u] = make_uint2(p.node_root[u], p.node_loc[u]);
+  rt_status st = dalloc(&s->d_meta, sizeof(uint2) * meta.size());
+  if (st == RT_OK) st = dalloc(&s->d_images, store.size());
+  if (st == RT_OK) st = dalloc(&s->d_image_off, sizeof(unsigned long long) * (n + 1));
+  if (st == RT_OK) st = dalloc(&s->d_roots, sizeof(uint32_t) * n);
+  if (st == RT_OK) st = dalloc(&s->d_member_first, sizeof(unsigned long long) * (n + 1));
+  if (st == RT_OK) st = dalloc(&s->d_member_bytes, sizeof(uint16_t) * p.member_bytes.size());
+  if (st != RT_OK) {
+    free_treelets(s);
+    return st;
+  }
+  std::vector<unsigned long long> off(p.image_off.begin(), p.image_off.end());
+  std::vector<unsigned long long> mf(p.member_first.begin(), p.member_first.end());
+  RT_CUDA(cudaMemcpy(s->d_meta, meta.data(), sizeof(uint2) * meta.size(), cudaMemcpyHostToDevice));
+  if (!store.empty()) RT_CUDA(cudaMemcpy(s->d_images, store.data(), store.size(), cudaMemcpyHostToDevice));
+  RT_CUDA(cudaMemcpy(s->d_image_off, off.data(), sizeof(unsigned long long) * off.size(), cudaMemcpyHostToDevice));
+  if (n) RT_CUDA(cudaMemcpy(s->d_roots, p.roots.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+  RT_CUDA(cudaMemcpy(s->d_member_first, mf.data(), sizeof(unsigned long long) * mf.size(), cudaMemcpyHostToDevice));
+  if (!p.member_bytes.empty())
+    RT_CUDA(cudaMemcpy(s->d_member_bytes, p.member_bytes.data(), sizeof(uint16_t) * p.member_bytes.size(),
+                       cudaMemcpyHostToDevice));
+  s->slot_bytes = (p.largest_image + 127u) & ~127u;
+  s->part = std::move(p);
+  s->has_treelets = true;
+  if (info) {
+    info->n_treelets = n;
+    info->max_treelet_bytes = max_treelet_bytes;
+    info->member_entries = s->part.members.size();
+    info->image_bytes = s->part.image_bytes;
+    info->largest_image = s->part.largest_image;
+    info->reserved = 0;
+  }
+  return RT_OK;
+}
+
+rt_status rt_treelets_get(const rt_scene* s, uint32_t* roots, uint64_t* member_first, uint32_t* members,
+                          uint16_t* member_bytes, uint32_t* node_root) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_treelets_get: NULL scene");
+  if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_treelets_get: treelets not formed");
+  const rtt::Partition& p = s->part;
+  if (roots) std::copy(p.roots.begin(), p.roots.end(), roots);
+  if (member_first) std::copy(p.member_first.begin(), p.member_first.end(), member_first);
+  if (members) std::copy(p.members.begin(), p.members.end(), members);
+  if (member_bytes) std::copy(p.member_bytes.begin(), p.member_bytes.end(), member_bytes);
+  if (node_root) std::copy(p.node_root.begin(), p.node_root.end(), node_root);
+  return RT_OK;
+}
+
+rt_status rt_treelets_remap(const rt_scene* s, uint32_t stride, uint64_t* new_addr) {
+  if (!s || !new_addr) return rti::fail(RT_ERR_INVALID, "rt_treelets_remap: NULL argument");
+  if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_treelets_remap: treelets not formed");
+  std::vector<uint64_t> m;
+  std::string err;
+  if (!rtt::remap_layout(s->part, s->n_units, stride, m, &err)) return rti::fail(RT_ERR_STATE, err);
+  std::copy(m.begin(), m.end(), new_addr);
+  return RT_OK;
+}
+
+rt_status rt_scene_set_tuning(rt_scene* s, const rt_tuning* t) {
+  if (!s || !t) return rti::fail(RT_ERR_INVALID, "rt_scene_set_tuning: NULL");
+  rt_tuning n = s->tuning;
+  auto ok_threads = [](uint32_t v) { return v >= 32 && v <= 256 && v % 32 == 0; };
+  if (t->block_threads) {
+    if (!ok_threads(t->block_threads)) return rti::fail(RT_ERR_INVALID, "block_threads must be 32..256, multiple of 32");
+    n.block_threads = t->block_threads;
+  }
+  if (t->staged_threads) {
+    if (!ok_threads(t->staged_threads)) return rti::fail(RT_ERR_INVALID, "staged_threads must be 32..256, multiple of 32");
+    n.staged_threads = t->staged_threads;
+  }
+  if (t->staged_epoch) n.staged_epoch = t->staged_epoch;
+  if (t->staged_slots) {
+    if (t->staged_slots > (uint32_t)rtk::kMaxSlots) return rti::fail(RT_ERR_INVALID, "staged_slots above 32");
+    n.staged_slots = t->staged_slots;
+  }
+  s->tuning = n;
+  return RT_OK;
+}
+
+rt_status rt_scene_get_tuning(const rt_scene* s, rt_tuning* t) {
+  if (!s || !t) return rti::fail(RT_ERR_INVALID, "rt_scene_get_tuning: NULL");
+  *t = s->tuning;
+  return RT_OK;
+}
+
+rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t n,
+                   uint32_t mode, rt_hit* hits, const rt_trace_buf* trace, void* stream) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_trace: NULL scene");
+  if (n == 0) return RT_OK;
+  if (!rays || !hits) return rti::fail(RT_ERR_INVALID, "rt_trace: NULL rays or hits");
+  if (mode > RT_MODE_STAGED) return rti::fail(RT_ERR_INVALID, "rt_trace: unknown mode");
+  const bool want_tl = trace && trace->treelets;
+  if ((mode != RT_MODE_PLAIN || want_tl) && !s->has_treelets)
+    return rti::fail(RT_ERR_STATE, "rt_trace: call rt_treelets_form first");
+  if (trace && (trace->visits || trace->treelets) && trace->capacity == 0)
+    return rti::fail(RT_ERR_INVALID, "rt_trace: trace capacity is 0");
+  cudaStream_t st = (cudaStream_t)stream;
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  rtk::TraceArgs a{};
+  a.blob = reinterpret_cast<const uint4*>(s->d_blob);
+  a.n_units = s->n_units;
+  a.rays = rays;
+  a.flags = flags;
+  a.default_flags = default_flags;
+  a.n = n;
+  a.hits = hits;
+  a.visits = trace ? trace->visits : nullptr;
+  a.tl_trace = trace ? trace->treelets : nullptr;
+  a.cap = (trace && (trace->visits || trace->treelets)) ? trace->capacity : 0;
+  a.meta = s->d_meta;
+  a.images = reinterpret_cast<const uint4*>(s->d_images);
+  a.image_off = s->d_image_off;
+  a.n_treelets = s->has_treelets ? (uint32_t)s->part.roots.size() : 0;
+  a.stats = s->d_stats;
+  a.status = s->d_status;
+  a.epoch = s->tuning.staged_epoch;
+  RT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, st));
+  RT_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), st));
+  if (mode == RT_MODE_PLAIN) {
+    const uint32_t bt = s->tuning.block_threads;
+    rtk::trace_plain_kernel<kPlainCap><<<(n + bt - 1) / bt, bt, 0, st>>>(a);
+  } else if (mode == RT_MODE_TREELET) {
+    const uint32_t bt = s->tuning.block_threads;
+    rtk::trace_treelet_kernel<kTreeletCap><<<(n + bt - 1) / bt, bt, 0, st>>>(a);
+  } else {
+    if (s->part.roots.size() >= rtt::kMaxDense)
+      return rti::fail(RT_ERR_TOO_LARGE, "rt_trace: too many treelets for staged mode (max 4194304)");
+    const uint32_t bt = s->tuning.staged_threads;
+    uint32_t slots = s->tuning.staged_slots;
+    const int limit = max_smem_per_block() - (int)sizeof(rtk::StagedShared) - 1024;
+    while (slots > 0 && (int)(slots * s->slot_bytes + 128) > limit) --slots;
+    a.slots = slots;
+    a.slot_bytes = s->slot_bytes;
+    const size_t dyn = (size_t)slots * s->slot_bytes + 128;
+    auto kern = rtk::trace_staged_kernel<kTreeletCap>;
+    RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    kern<<<(n + bt - 1) / bt, bt, dyn, st>>>(a);
+  }
+  RT_CUDA(cudaGetLastError());
+  return RT_OK;
+}
+
+rt_status rt_trace_stats_get(rt_scene* s, rt_trace_stats* out) {
+  if (!s || !out) return rti::fail(RT_ERR_INVALID, "rt_trace_stats_get: NULL");
+  unsigned long long v[rtk::ST_COUNT];
+  uint32_t status = 0;
+  RT_CUDA(cudaMemcpy(v, s->d_stats, sizeof(v), cudaMemcpyDeviceToHost));
+  RT_CUDA(cudaMemcpy(&status, s->d_status, sizeof(status), cudaMemcpyDeviceToHost));
+  out->node_bytes = v[rtk::ST_NODE_BYTES];
+  out->staged_bytes = v[rtk::ST_STAGED_BYTES];
+  out->smem_reads = v[rtk::ST_SMEM_READS];
+  out->gmem_reads = v[rtk::ST_GMEM_READS];
+  out->stagings = v[rtk::ST_STAGINGS];
+  out->device_status = status;
+  return RT_OK;
+}
+
+rt_status rt_trace_host(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t n,
+                        uint32_t mode, rt_hit* hits, const rt_trace_buf* trace) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_trace_host: NULL scene");
+  if (n == 0) return RT_OK;
+  if (!rays || !hits) return rti::fail(RT_ERR_INVALID, "rt_trace_host: NULL rays or hits");
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  const uint32_t cap = (trace && (trace->visits || trace->treelets)) ? trace->capacity : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t b_rays = al(sizeof(rt_ray) * (size_t)n), b_flags = flags ? al(sizeof(uint32_t) * (size_t)n) : 0;
+  const size_t b_hits = al(sizeof(rt_hit) * (size_t)n);
+  const size_t b_vis = (trace && trace->visits) ? al(sizeof(uint32_t) * (size_t)n * cap) : 0;
+  const size_t b_tl = (trace && trace->treelets) ? al(sizeof(uint32_t) * (size_t)n * cap) : 0;
+  const size_t need = b_rays + b_flags + b_hits + b_vis + b_tl;
+  if (need > s->io_bytes) {
+    cudaFree(s->d_io);
+    s->d_io = nullptr;
+    s->io_bytes = 0;
+    rt_status st = dalloc((uint8_t**)&s->d_io, need);
+    if (st != RT_OK) return st;
+    s->io_bytes = need;
+  }
+  uint8_t* base = (uint8_t*)s->d_io;
+  rt_ray* d_rays = (rt_ray*)base;
+  uint32_t* d_flags = flags ? (uint32_t*)(base + b_rays) : nullptr;
+  rt_hit* d_hits = (rt_hit*)(base + b_rays + b_flags);
+  uint32_t* d_vis = b_vis ? (uint32_t*)(base + b_rays + b_flags + b_hits) : nullptr;
+  uint32_t* d_tl = b_tl ? (uint32_t*)(base + b_rays + b_flags + b_hits + b_vis) : nullptr;
+  RT_CUDA(cudaMemcpyAsync(d_rays, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  if (flags) RT_CUDA(cudaMemcpyAsync(d_flags, flags, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  rt_trace_buf tb{d_vis, d_tl, cap};
+  rt_status st = rt_trace(s, d_rays, d_flags, default_flags, n, mode, d_hits, cap ? &tb : nullptr, s->stream);
+  if (st != RT_OK) return st;
+  RT_CUDA(cudaMemcpyAsync(hits, d_hits, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  if (d_vis)
+    RT_CUDA(cudaMemcpyAsync(trace->visits, d_vis, sizeof(uint32_t) * (size_t)n * cap, cudaMemcpyDeviceToHost, s->stream));
+  if (d_tl)
+    RT_CUDA(cudaMemcpyAsync(trace->treelets, d_tl, sizeof(uint32_t) * (size_t)n * cap, cudaMemcpyDeviceToHost,
+                            s->stream));
+  RT_CUDA(cudaStreamSynchronize(s->stream));
+  return RT_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ bounce rays
+namespace {
+
+__global__ void bounce_kernel(const uint4* blob, uint32_t n_units, const rt_ray* rays, const rt_hit* hits, uint32_t n,
+                              uint64_t seed, float tmin, float tmax, rt_ray* out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const rt_hit h = hits[i];
+  const rt_ray ray = rays[i];
+  rt_ray o;
+  if (!h.hit_geometry || h.closest_leaf >= n_units || h.closest_instance + 1 >= n_units) {
+    o = ray;
+    o.tmin = 1.0f;
+    o.tmax = 0.0f;
+    out[i] = o;
+    return;
+  }
+  rti::BounceInput in;
+  uint4* lp = reinterpret_cast<uint4*>(in.leaf);
+  uint4* ip = reinterpret_cast<uint4*>(in.inst);
+  for (int q = 0; q < 4; ++q) lp[q] = blob[(uint64_t)h.closest_leaf * 4 + q];
+  for (int q = 0; q < 8; ++q) ip[q] = blob[(uint64_t)h.closest_instance * 4 + q];
+  rti::make_bounce(in, ray, h, seed, i, tmin, tmax, o);
+  out[i] = o;
+}
+
+}  // namespace
+
+extern "C" rt_status rt_gen_bounce_rays(rt_scene* s, const rt_ray* rays, const rt_hit* hits, uint32_t n, uint64_t seed,
+                                        float tmin, float tmax, rt_ray* out, void* stream) {
+  if (!s || !rays || !hits || !out) return rti::fail(RT_ERR_INVALID, "rt_gen_bounce_rays: NULL argument");
+  if (n == 0) return RT_OK;
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  bounce_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const uint4*>(s->d_blob),
+                                                                     s->n_units, rays, hits, n, seed, tmin, tmax, out);
+  RT_CUDA(cudaGetLastError());
+  return RT_OK;
+}
+
+extern "C" rt_status rt_prefetch_decide(rt_scene* s, const uint32_t* next_unit, uint32_t n_units, uint32_t lanes,
+                                        const rt_prefetch_params* params, rt_prefetch_state* state,
+                                        rt_prefetch_decision* out, void* stream) {
+  if (!s || !next_unit || !params || !state || !out) return rti::fail(RT_ERR_INVALID, "rt_prefetch_decide: NULL");
+  if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_prefetch_decide: call rt_treelets_form first");
+  if (lanes == 0 || lanes > (uint32_t)rtk::kMaxLanes)
+    return rti::fail(RT_ERR_TOO_LARGE, "rt_prefetch_decide: lanes must be 1..1024");
+  if (params->heuristic > RT_PREFETCH_LATTER) return rti::fail(RT_ERR_INVALID, "rt_prefetch_decide: unknown heuristic");
+  if (n_units == 0) return RT_OK;
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  rtk::PrefetchArgs a{};
+  a.next_unit = next_unit;
+  a.n_groups = n_units;
+  a.lanes = lanes;
+  a.p = *params;
+  a.state = state;
+  a.out = out;
+  a.meta = s->d_meta;
+  a.n_units = s->n_units;
+  a.roots = s->d_roots;
+  a.member_first = s->d_member_first;
+  a.member_bytes = s->d_member_bytes;
+  a.n_treelets = (uint32_t)s->part.roots.size();
+  rtk::prefetch_decide_kernel<<<n_units, 512, 0, (cudaStream_t)stream>>>(a);
+  RT_CUDA(cudaGetLastError());
+  return RT_OK;
+}

@@ -1,0 +1,108 @@
+// Device-side node access: 16-byte vector loads of the 64 / 128-byte nodes
+// from global memory (read-only path) or from a staged shared-memory image,
+// and the decoders for the fields the walk uses (format.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "format.h"
+#include "rtmath.h"
+
+namespace rtd {
+
+// Raw node words.  Internal nodes and quad leaves use 16 words (64 B).
+struct Node64 {
+  uint32_t w[16];
+};
+
+__device__ __forceinline__ uint4 ld_global_nc(const uint4* p) { return __ldg(p); }
+
+__device__ __forceinline__ uint4 ld_shared_v4(uint32_t saddr) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(saddr));
+  return v;
+}
+
+// Loads 64 bytes: from shared memory when saddr != 0, else from global.
+__device__ __forceinline__ void load64(const uint4* g, uint32_t saddr, Node64& n) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uint4 v = saddr ? ld_shared_v4(saddr + 16u * q) : ld_global_nc(g + q);
+    n.w[4 * q + 0] = v.x;
+    n.w[4 * q + 1] = v.y;
+    n.w[4 * q + 2] = v.z;
+    n.w[4 * q + 3] = v.w;
+  }
+}
+
+__device__ __forceinline__ uint4 load16(const uint4* g, uint32_t saddr, int q) {
+  return saddr ? ld_shared_v4(saddr + 16u * q) : ld_global_nc(g + q);
+}
+
+__device__ __forceinline__ uint32_t byte_at(const Node64& n, int b) { return (n.w[b >> 2] >> ((b & 3) * 8)) & 0xffu; }
+__device__ __forceinline__ float f32_at(const Node64& n, int b) { return __uint_as_float(n.w[b >> 2]); }
+
+// Result of testing one internal node's children against a ray.
+struct ChildHits {
+  uint32_t hit_mask;    // bit i: child i hit and not culled
+  uint32_t child_unit;  // unit index of child 0's block
+  uint32_t info;        // 6 x 6-bit child info (bits 0-1 size, 2-5 type), child i at bits 6i
+};
+
+// The box tests of an internal node (vulkan_ray_tracing.cc:2518-2553 and the
+// bottom-level twin :2714-2741): children with ChildSize > 0 are slab-tested
+// with the ray's [tmin, tmax]; a hit at thit >= cull is dropped.
+__device__ __forceinline__ ChildHits test_children(const Node64& n, uint32_t node_unit, rtm::V3 o, rtm::V3 idir,
+                                                   float tmin, float tmax, float cull) {
+  ChildHits r;
+  const float ox = f32_at(n, 0), oy = f32_at(n, 4), oz = f32_at(n, 8);
+  const int child_off = (int)n.w[3];
+  const int ex = (int)(int8_t)byte_at(n, 18), ey = (int)(int8_t)byte_at(n, 19), ez = (int)(int8_t)byte_at(n, 20);
+  const float sx = rtm::exp2_int(ex - 8), sy = rtm::exp2_int(ey - 8), sz = rtm::exp2_int(ez - 8);
+  r.hit_mask = 0;
+  r.info = 0;
+  r.child_unit = (uint32_t)((int)node_unit + child_off);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const uint32_t info = byte_at(n, 22 + i) & 0x3fu;
+    r.info |= info << (6 * i);
+    if (info & 3u) {
+      rtm::V3 lo, hi;
+      lo.x = ox + (float)byte_at(n, rtf::IN_LO_X + i) * sx;
+      lo.y = oy + (float)byte_at(n, rtf::IN_LO_Y + i) * sy;
+      lo.z = oz + (float)byte_at(n, rtf::IN_LO_Z + i) * sz;
+      hi.x = ox + (float)byte_at(n, rtf::IN_HI_X + i) * sx;
+      hi.y = oy + (float)byte_at(n, rtf::IN_HI_Y + i) * sy;
+      hi.z = oz + (float)byte_at(n, rtf::IN_HI_Z + i) * sz;
+      float thit;
+      bool h = rtm::ray_box_test(lo, hi, idir, o, tmin, tmax, thit);
+      if (h && thit >= cull) h = false;
+      if (h) r.hit_mask |= 1u << i;
+    }
+  }
+  return r;
+}
+
+// Instance leaf fields used by the walk.
+struct Instance {
+  rtm::Mat43 w2o;
+  uint64_t bvh_address;
+  uint32_t instance_id;
+};
+
+__device__ __forceinline__ void load_instance(const uint4* g, uint32_t saddr, Instance& in) {
+  const uint4 a = load16(g, saddr, 1), b = load16(g, saddr, 2), c = load16(g, saddr, 3);
+  const uint4 d = load16(g, saddr, 4), e = load16(g, saddr, 7);
+  // bytes 16..51: world-to-object rows 0-2
+  const uint32_t lin[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) in.w2o.m[k / 3][k % 3] = __uint_as_float(lin[k]);
+  // bytes 116..127: translation row as the reference's struct-order read takes it
+  in.w2o.m[3][0] = __uint_as_float(e.y);
+  in.w2o.m[3][1] = __uint_as_float(e.z);
+  in.w2o.m[3][2] = __uint_as_float(e.w);
+  in.bvh_address = (uint64_t)d.x | ((uint64_t)d.y << 32);
+  in.instance_id = d.z;
+}
+
+}  // namespace rtd

@@ -1,0 +1,307 @@
+// Traversal kernels.
+//
+//   trace_plain_kernel    traceRay order (vulkan_ray_tracing.cc:2309-3076)
+//   trace_treelet_kernel  traceRayWithTreelets order (vulkan_ray_tracing.cc:1522-2307);
+//                         with STAGED = true, each CTA votes every epoch on the
+//                         treelet most of its rays need next (the treelet-prefetch
+//                         decision of shader.cc:3419-3441 with heuristic ALWAYS),
+//                         copies that treelet's image into shared memory with
+//                         cp.async.bulk, and serves node reads that fall in a
+//                         resident treelet from shared memory.  Staging changes
+//                         where a node's bytes come from, never which nodes a
+//                         ray visits or in which order.
+//
+// One thread walks one ray, with its stack(s) in local memory.  Each thread
+// keeps the reference's visit order exactly; FP32 arithmetic keeps the
+// reference's operation order and is compiled without FMA contraction.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/treelet_rt.h"
+#include "device_nodes.cuh"
+#include "format.h"
+#include "rtmath.h"
+
+namespace rtk {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t kTop = 2u, kLeaf = 1u;  // stack entry = unit << 2 | top | leaf
+
+// Device counters, all uint64.
+enum Stat { ST_NODE_BYTES = 0, ST_STAGED_BYTES, ST_SMEM_READS, ST_GMEM_READS, ST_STAGINGS, ST_COUNT };
+// Status word bits set by kernels (device-wide, not per ray).
+constexpr uint32_t kStatusTimeout = 1u;
+
+struct TraceArgs {
+  const uint4* blob;
+  uint32_t n_units;
+  const rt_ray* rays;
+  const uint32_t* flags;
+  uint32_t default_flags;
+  uint32_t n;
+  rt_hit* hits;
+  uint32_t* visits;
+  uint32_t* tl_trace;
+  uint32_t cap;
+  const uint2* meta;           // per unit: x = treelet root unit, y = dense << 10 | slot
+  const uint4* images;         // staged image store
+  const unsigned long long* image_off;  // per dense treelet, n_treelets + 1
+  uint32_t n_treelets;
+  unsigned long long* stats;   // ST_COUNT counters
+  uint32_t* status;            // kStatus* bits
+  uint32_t slots;              // staged treelet slots per CTA
+  uint32_t slot_bytes;         // bytes per slot (multiple of 128)
+  uint32_t epoch;              // node visits per ray between votes
+};
+
+struct Recorder {
+  uint32_t* vrow;
+  uint32_t* trow;
+  uint32_t cap;
+  uint32_t n;
+  uint32_t bytes;
+  const uint2* meta;
+  __device__ __forceinline__ void rec(uint32_t unit, uint32_t type) {
+    if (n < cap) {
+      if (vrow) vrow[n] = rtf::pack_visit(unit, type);
+      if (trow) trow[n] = meta[unit].x;
+    }
+    n++;
+    bytes += rtf::tx_bytes(type);
+  }
+};
+
+__device__ __forceinline__ void load_ray(const rt_ray* rays, uint32_t r, rtm::V3& o, float& tmin, rtm::V3& d,
+                                         float& tmax) {
+  const float4* p = reinterpret_cast<const float4*>(rays + r);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  o = rtm::v3(a.x, a.y, a.z);
+  tmin = a.w;
+  d = rtm::v3(b.x, b.y, b.z);
+  tmax = b.w;
+}
+
+// Hit record from the closest leaf / instance (vulkan_ray_tracing.cc:2990-3028).
+__device__ __forceinline__ void write_hit(const TraceArgs& a, uint32_t r, bool hit, float min_thit, rtm::V3 O,
+                                          rtm::V3 D, float tmin, float tmax, uint32_t c_leaf, uint32_t c_inst,
+                                          float c_tobj, const Recorder& rec, uint32_t status) {
+  rt_hit h;
+  h.hit_geometry = 0;
+  h.geometry_index = 0;
+  h.primitive_index = 0;
+  h.instance_index = 0;
+  h.world_min_thit = 0.0f;
+  h.barycentric[0] = h.barycentric[1] = h.barycentric[2] = 0.0f;
+  h.intersection_point[0] = h.intersection_point[1] = h.intersection_point[2] = 0.0f;
+  h.closest_leaf = 0;
+  h.closest_instance = 0;
+  h.reserved = 0;
+  if (hit) {
+    rtd::Node64 q;
+    rtd::load64(a.blob + (uint64_t)c_leaf * 4, 0, q);
+    rtd::Instance in;
+    rtd::load_instance(a.blob + (uint64_t)c_inst * 4, 0, in);
+    const rtm::ObjRay orr = rtm::make_transformed_ray(in.w2o, O, D, tmin, tmax);
+    h.hit_geometry = 1;
+    h.geometry_index = rtf::geometry_index_of(q.w[1]);
+    h.primitive_index = q.w[2];
+    h.instance_index = in.instance_id;
+    h.world_min_thit = min_thit;
+    h.intersection_point[0] = O.x + D.x * min_thit;
+    h.intersection_point[1] = O.y + D.y * min_thit;
+    h.intersection_point[2] = O.z + D.z * min_thit;
+    const rtm::V3 p = rtm::v3(orr.o.x + orr.d.x * c_tobj, orr.o.y + orr.d.y * c_tobj, orr.o.z + orr.d.z * c_tobj);
+    const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
+    const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
+    const rtm::V3 v2 = rtm::v3(__uint_as_float(q.w[10]), __uint_as_float(q.w[11]), __uint_as_float(q.w[12]));
+    const rtm::V3 b = rtm::barycentric(p, v0, v1, v2);
+    h.barycentric[0] = b.x;
+    h.barycentric[1] = b.y;
+    h.barycentric[2] = b.z;
+    h.closest_leaf = c_leaf;
+    h.closest_instance = c_inst;
+  }
+  h.n_visits = rec.n;
+  h.status = status | (rec.cap && rec.n > rec.cap ? RT_RAY_TRACE_OVERFLOW : 0u);
+  a.hits[r] = h;
+}
+
+// Object-space ray of one instance (make_transformed_ray).
+struct InstCtx {
+  uint32_t unit;
+  rtm::V3 o, d, idir;
+  float tmin, tmax, mult;
+};
+
+__device__ __forceinline__ void enter_instance(const rtd::Instance& in, uint32_t unit, rtm::V3 O, rtm::V3 D, float tmin,
+                                               float tmax, InstCtx& c) {
+  const rtm::ObjRay r = rtm::make_transformed_ray(in.w2o, O, D, tmin, tmax);
+  c.unit = unit;
+  c.o = r.o;
+  c.d = r.d;
+  c.tmin = r.tmin;
+  c.tmax = r.tmax;
+  c.mult = r.mult;
+  c.idir = rtm::calculate_idir(r.d);
+}
+
+// Adds v summed over the calling warp's active lanes with one atomic.
+__device__ __forceinline__ void add_warp_total(unsigned long long* dst, uint32_t v) {
+  const uint32_t mask = __activemask();
+  const uint32_t sum = __reduce_add_sync(mask, v);
+  if ((threadIdx.x & 31u) == (uint32_t)(__ffs(mask) - 1)) atomicAdd(dst, (unsigned long long)sum);
+}
+
+// ----------------------------------------------------------------- plain
+template <int CAP>
+__global__ void __launch_bounds__(256) trace_plain_kernel(TraceArgs a) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.n) return;
+  rtm::V3 O, D;
+  float tmin, tmax;
+  load_ray(a.rays, r, O, tmin, D, tmax);
+  const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
+  const bool terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
+  const bool opaque = flags & rtf::RAY_FLAG_OPAQUE;
+  Recorder rec{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
+               a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, a.meta};
+  uint32_t status = 0;
+  uint32_t stk[CAP];
+  int sp = 0;
+  float min_thit = tmax;
+  uint32_t c_leaf = 0, c_inst = 0;
+  float c_tobj = 0.0f;
+  const rtm::V3 idir = rtm::calculate_idir(D);
+
+  rec.rec(0, rtf::TX_STRUCTURE);
+  {
+    const uint4 h0 = __ldg(a.blob), h1 = __ldg(a.blob + 1);
+    const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
+    const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
+    const rtm::V3 bmax = rtm::v3(__uint_as_float(h1.y), __uint_as_float(h1.z), __uint_as_float(h1.w));
+    float th;
+    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) stk[sp++] = ((uint32_t)(root_off >> 6) << 2) | kTop;
+  }
+  uint32_t next = kNone;
+  bool inblas = false;
+  InstCtx ic;
+  ic.unit = kNone;
+  for (;;) {
+    if (next != kNone) {
+      const uint32_t unit = next;
+      if (unit >= a.n_units) {
+        status |= RT_RAY_BAD_NODE;
+        break;
+      }
+      rec.rec(unit, rtf::TX_INTERNAL);
+      rtd::Node64 nd;
+      rtd::load64(a.blob + (uint64_t)unit * 4, 0, nd);
+      const rtd::ChildHits ch = inblas ? rtd::test_children(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, min_thit * ic.mult)
+                                       : rtd::test_children(nd, unit, O, idir, tmin, tmax, min_thit);
+      const uint32_t level = inblas ? 0u : kTop;
+      uint32_t c = ch.child_unit;
+      uint32_t nn = kNone;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        const uint32_t info = (ch.info >> (6 * i)) & 0x3fu;
+        if ((ch.hit_mask >> i) & 1u) {
+          if ((info >> 2) != rtf::CT_INTERNAL) {
+            if (sp < CAP) stk[sp++] = (c << 2) | level | kLeaf;
+            else status |= RT_RAY_STACK_OVERFLOW;
+          } else if (nn == kNone) {
+            nn = c;
+          } else {
+            if (sp < CAP) stk[sp++] = (c << 2) | level;
+            else status |= RT_RAY_STACK_OVERFLOW;
+          }
+        }
+        c += info & 3u;
+      }
+      if (status & RT_RAY_STACK_OVERFLOW) break;
+      next = nn;
+      continue;
+    }
+    if (inblas) {
+      if (sp > 0 && !(stk[sp - 1] & kTop)) {
+        const uint32_t e = stk[--sp];
+        const uint32_t unit = e >> 2;
+        if (!(e & kLeaf)) {
+          next = unit;
+          continue;
+        }
+        if (unit >= a.n_units) {
+          status |= RT_RAY_BAD_NODE;
+          break;
+        }
+        rec.rec(unit, rtf::TX_LEAF_DESC);
+        rtd::Node64 q;
+        rtd::load64(a.blob + (uint64_t)unit * 4, 0, q);
+        if (rtf::leaf_type_of(q.w[1]) == 0) {
+          const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
+          const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
+          const rtm::V3 v2 = rtm::v3(__uint_as_float(q.w[10]), __uint_as_float(q.w[11]), __uint_as_float(q.w[12]));
+          float t = 0.0f;
+          const bool hit = rtm::ray_triangle_test(v0, v1, v2, ic.o, ic.d, t);
+          const float wt = t / ic.mult;
+          if (hit && tmin <= wt && wt <= tmax) {
+            if (opaque && wt < min_thit) min_thit = t / ic.mult;
+            c_leaf = unit;
+            c_inst = ic.unit;
+            c_tobj = t;
+            rec.rec(unit, rtf::TX_QUAD_LEAF_HIT);
+            if (terminate) sp = 0;
+          } else {
+            rec.rec(unit, rtf::TX_QUAD_LEAF);
+          }
+        } else {
+          status |= RT_RAY_HIT_PROCEDURAL;
+          rec.rec(unit, rtf::TX_PROCEDURAL_LEAF);
+        }
+        continue;
+      }
+      inblas = false;
+      continue;
+    }
+    if (sp == 0) break;
+    const uint32_t e = stk[--sp];
+    const uint32_t unit = e >> 2;
+    if (!(e & kLeaf)) {
+      next = unit;
+      continue;
+    }
+    // instance leaf (vulkan_ray_tracing.cc:2602-2676)
+    if (unit + 1 >= a.n_units) {
+      status |= RT_RAY_BAD_NODE;
+      break;
+    }
+    rec.rec(unit, rtf::TX_INSTANCE_LEAF);
+    rtd::Instance in;
+    rtd::load_instance(a.blob + (uint64_t)unit * 4, 0, in);
+    const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
+    if ((hdr & 63) || hdr / 64 >= a.n_units) {
+      status |= RT_RAY_BAD_NODE;
+      break;
+    }
+    rec.rec((uint32_t)(hdr >> 6), rtf::TX_STRUCTURE);
+    const uint4 h0 = __ldg(a.blob + (hdr >> 4));
+    const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
+    enter_instance(in, unit, O, D, tmin, tmax, ic);
+    if (sp < CAP) {
+      stk[sp++] = (uint32_t)(broot >> 6) << 2;
+    } else {
+      status |= RT_RAY_STACK_OVERFLOW;
+      break;
+    }
+    inblas = true;
+  }
+  const bool hit = min_thit < tmax;
+  if (status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE)) {
+    write_hit(a, r, false, min_thit, O, D, tmin, tmax, 0, 0, 0.0f, rec, status);
+  } else {
+    write_hit(a, r, hit, min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
+  }
+  if (a.stats) add_warp_total(a.stats + ST_NODE_BYTES, rec.bytes);
+}
+
+}  // namespace rtk
