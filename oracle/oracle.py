@@ -116,6 +116,11 @@ def trace(blob: np.ndarray, rays: np.ndarray, mode: int = 0, treelets: Treelets 
           threads: int = 1):
     """mode 0 = traceRay, 1 = traceRayWithTreelets.  Returns (hits, visits, treelet ids)."""
     blob = np.ascontiguousarray(blob, np.uint8)
+    if treelets is not None:
+        # the partition is keyed by node addresses inside its own copy of the blob
+        if blob.nbytes != treelets.blob.nbytes or not np.array_equal(blob, treelets.blob):
+            raise OracleError("trace: blob differs from the one the treelets were formed on")
+        blob = treelets.blob
     rays = np.ascontiguousarray(rays, RAY_DTYPE)
     n = len(rays)
     hits = np.zeros(n, HIT_DTYPE)

@@ -46,7 +46,8 @@ __device__ __forceinline__ float f32_at(const Node64& n, int b) { return __uint_
 struct ChildHits {
   uint32_t hit_mask;    // bit i: child i hit and not culled
   uint32_t child_unit;  // unit index of child 0's block
-  uint32_t info;        // 6 x 6-bit child info (bits 0-1 size, 2-5 type), child i at bits 6i
+  uint64_t info;        // child i's info byte (bits 0-1 size, 2-5 type) at bits 8i..8i+7
+  __device__ __forceinline__ uint32_t info_of(int i) const { return (uint32_t)(info >> (8 * i)) & 0x3fu; }
 };
 
 // The box tests of an internal node (vulkan_ray_tracing.cc:2518-2553 and the
@@ -65,7 +66,7 @@ __device__ __forceinline__ ChildHits test_children(const Node64& n, uint32_t nod
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
     const uint32_t info = byte_at(n, 22 + i) & 0x3fu;
-    r.info |= info << (6 * i);
+    r.info |= (uint64_t)info << (8 * i);
     if (info & 3u) {
       rtm::V3 lo, hi;
       lo.x = ox + (float)byte_at(n, rtf::IN_LO_X + i) * sx;

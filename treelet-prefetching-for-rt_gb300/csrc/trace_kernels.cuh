@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) trace_plain_kernel(TraceArgs a) {
       uint32_t nn = kNone;
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        const uint32_t info = (ch.info >> (6 * i)) & 0x3fu;
+        const uint32_t info = ch.info_of(i);
         if ((ch.hit_mask >> i) & 1u) {
           if ((info >> 2) != rtf::CT_INTERNAL) {
             if (sp < CAP) stk[sp++] = (c << 2) | level | kLeaf;

@@ -132,7 +132,7 @@ struct Walker {
       uint32_t c = ch.child_unit;
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        const uint32_t info = (ch.info >> (6 * i)) & 0x3fu;
+        const uint32_t info = ch.info_of(i);
         if ((ch.hit_mask >> i) & 1u) {
           const uint32_t lf = ((info >> 2) != rtf::CT_INTERNAL) ? kLeaf : 0u;
           route(a, (c << 2) | level | lf, inst);
