@@ -229,6 +229,22 @@ rt_status rt_trace(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, u
 rt_status rt_trace_host(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                         uint32_t n, uint32_t mode, rt_hit* hits, const rt_trace_buf* trace);
 
+/* rt_trace_host for callers that cannot allocate device memory: no
+ * counterpart in the reference.  A simulator calling the traversal per warp
+ * from its cycle loop, or a process whose device memory belongs to its own
+ * allocator, cannot have the library cudaMalloc a staging buffer (an
+ * allocation synchronises the device).  This call stages rays, flags and hit
+ * records through one fixed device array of 3,276,800 bytes that the library
+ * reserves at load time (held on every GPU that loads it until exit), so it
+ * takes at most RT_NOALLOC_MAX_RAYS rays per call and returns
+ * RT_ERR_TOO_LARGE above that.  All calls on a device share the array:
+ * calls that overlap on the GPU race, so serialise them.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * No visit traces.  Synchronous. */
+#define RT_NOALLOC_MAX_RAYS 32768u
+rt_status rt_trace_host_noalloc(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
+                                uint32_t n, uint32_t mode, rt_hit* hits);
+
 /* Traversal tuning: stack entries per ray, threads per block, rays per
  * staging epoch.  0 keeps the current value. */
 typedef struct rt_tuning {

@@ -16,10 +16,8 @@
 #include <stdint.h>
 #include "format.h"
 
-#if !defined(__CUDACC__)
 #include <cmath>
 #include <cstring>
-#endif
 
 namespace rtm {
 
