@@ -117,7 +117,7 @@ def make_workload(ctx_needed: bool = True):
     import treelet_rt as rt
 
     t0 = time.time()
-    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * WIDTH * HEIGHT, SEED)
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 1024 * 1024, SEED)
     cam = rt.default_camera(rt.SCENE_TERRAIN_INSTANCES)
     prim = rt.camera_rays(cam, WIDTH, HEIGHT, SPP, SEED, 1e-4, 1e30)
     return blob, prim, time.time() - t0
@@ -353,7 +353,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-sample", type=int, default=1000000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--size", default="full", choices=["full", "small"],
+                    help="small: the same scene with 512x512x1 primary rays + bounces (profiling case)")
     args = ap.parse_args()
+    if args.size == "small":
+        global WIDTH, HEIGHT, SPP, WORKLOAD
+        WIDTH = HEIGHT = 512
+        SPP = 1
+        WORKLOAD = WORKLOAD.replace("1024x1024x2spp", "512x512x1spp").replace("4,194,304", "524,288")
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     if args.impl == "reference":

@@ -209,6 +209,16 @@ rt_status rt_treelets_form(rt_scene* scene, uint32_t max_treelet_bytes, rt_treel
 rt_status rt_treelets_get(const rt_scene* scene, uint32_t* roots, uint64_t* member_first, uint32_t* members,
                           uint16_t* member_bytes, uint32_t* node_root);
 
+/* The same partition on the host only, without a device (for tools and
+ * tests): form, read back (same layout as rt_treelets_get), remap, free. */
+typedef struct rt_partition rt_partition;
+rt_status rt_partition_form(const rt_blob* blob, uint32_t max_treelet_bytes, rt_partition** out,
+                            rt_treelet_info* info);
+rt_status rt_partition_get(const rt_partition* p, uint32_t* roots, uint64_t* member_first, uint32_t* members,
+                           uint16_t* member_bytes, uint32_t* node_root);
+rt_status rt_partition_remap(const rt_partition* p, uint32_t stride, uint64_t* new_addr);
+void rt_partition_free(rt_partition* p);
+
 /* Treelet-contiguous relayout (remapBVHToTreeletLayout,
  * vulkan_ray_tracing.cc:1473-1509): new_addr[u] for every unit, or
  * 0xFFFFFFFFFFFFFFFF for units not placed; treelet k starts at

@@ -123,6 +123,42 @@ def bounce_rays_host(blob: Blob, rays: np.ndarray, hits: np.ndarray, seed: int =
     return out
 
 
+class Partition:
+    """The treelet partition of a blob, formed on the host (no device)."""
+
+    def __init__(self, blob: Blob, max_bytes: int):
+        h = C.c_void_p()
+        info = TreeletInfo()
+        check(lib().rt_partition_form(blob.handle, max_bytes, C.byref(h), C.byref(info)))
+        self._h = h
+        self.n_units = blob.nbytes() // 64
+        self.info = {k: getattr(info, k) for k, _ in TreeletInfo._fields_}
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().rt_partition_free(self._h)
+                self._h = C.c_void_p(0)
+        except Exception:
+            pass
+
+    def get(self) -> dict:
+        n, m = self.info["n_treelets"], self.info["member_entries"]
+        roots = np.zeros(n, np.uint32)
+        first = np.zeros(n + 1, np.uint64)
+        members = np.zeros(m, np.uint32)
+        mbytes = np.zeros(m, np.uint16)
+        node_root = np.zeros(self.n_units, np.uint32)
+        check(lib().rt_partition_get(self._h, roots.ctypes.data, first.ctypes.data, members.ctypes.data,
+                                     mbytes.ctypes.data, node_root.ctypes.data))
+        return dict(roots=roots, member_first=first, members=members, member_bytes=mbytes, node_root=node_root)
+
+    def remap(self, stride: int = 0) -> np.ndarray:
+        out = np.zeros(self.n_units, np.uint64)
+        check(lib().rt_partition_remap(self._h, stride, out.ctypes.data))
+        return out
+
+
 class Context:
     def __init__(self, device: int = 0):
         h = C.c_void_p()

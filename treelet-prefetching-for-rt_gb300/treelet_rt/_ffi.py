@@ -99,6 +99,11 @@ PROTOTYPES = {
     "rt_trace_stats_get": (C.c_int, [vp, C.POINTER(TraceStats)]),
     "rt_gen_bounce_rays": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint64, C.c_float, C.c_float, vp, vp]),
     "rt_prefetch_decide": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.POINTER(PrefetchParams), vp, vp, vp]),
+    "rt_partition_form": (C.c_int, [vp, C.c_uint32, C.POINTER(vp), C.POINTER(TreeletInfo)]),
+    "rt_partition_get": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+    "rt_partition_remap": (C.c_int, [vp, C.c_uint32, vp]),
+    "rt_partition_free": (None, [vp]),
+    "rt_trace_host_noalloc": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
 }
 
 _lib = None

@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off"] + ARCH
 
-HOST_SOURCES = ["builder.cpp", "scenes.cpp", "treelets.cpp"]
+HOST_SOURCES = ["builder.cpp", "scenes.cpp", "treelets.cpp", "partition_capi.cpp"]
 CUDA_SOURCES = ["capi.cu", "noalloc.cu"]
 
 
