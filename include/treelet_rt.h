@@ -255,13 +255,16 @@ rt_status rt_trace_host(rt_scene* scene, const rt_ray* rays, const uint32_t* fla
 rt_status rt_trace_host_noalloc(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                                 uint32_t n, uint32_t mode, rt_hit* hits);
 
-/* Traversal tuning: stack entries per ray, threads per block, rays per
- * staging epoch.  0 keeps the current value. */
+/* Traversal tuning; 0 keeps the current value.  None of these changes any
+ * result, only speed. */
 typedef struct rt_tuning {
-  uint32_t block_threads;   /* threads per CTA for RT_MODE_PLAIN / RT_MODE_TREELET */
-  uint32_t staged_threads;  /* threads per CTA for RT_MODE_STAGED */
-  uint32_t staged_epoch;    /* nodes a ray processes between staging decisions */
-  uint32_t staged_slots;    /* treelets resident in shared memory at once */
+  uint32_t block_threads;     /* threads per CTA for RT_MODE_PLAIN / RT_MODE_TREELET (32..256) */
+  uint32_t staged_threads;    /* threads per CTA for RT_MODE_STAGED (32..256) */
+  uint32_t staged_epoch;      /* node visits of a warp between staging votes */
+  uint32_t staged_slots;      /* shared-memory treelet slots per warp (1..8) */
+  uint32_t refill_lanes;      /* idle lanes of a warp that make it fetch new rays (1..32) */
+  uint32_t staged_slot_bytes; /* bytes per slot: a treelet's first bytes when smaller than it */
+  uint32_t staged_min_votes;  /* lanes of a warp that must want a treelet to stage it (1..32) */
 } rt_tuning;
 rt_status rt_scene_set_tuning(rt_scene* scene, const rt_tuning* t);
 rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);

@@ -119,9 +119,11 @@ def test_trace_overflow_truncates(ctx):
     assert (oh["status"] & rt.RAY_TRACE_OVERFLOW).any()
 
 
-@pytest.mark.parametrize("tuning", [dict(staged_slots=1, staged_epoch=1), dict(staged_slots=8, staged_epoch=4),
-                                    dict(staged_slots=16, staged_epoch=64, staged_threads=128),
-                                    dict(block_threads=64, staged_threads=64)])
+@pytest.mark.parametrize("tuning", [dict(staged_slots=1, staged_epoch=1, staged_min_votes=1),
+                                    dict(staged_slots=8, staged_epoch=4, staged_slot_bytes=1024),
+                                    dict(staged_slots=2, staged_epoch=64, staged_threads=256, staged_min_votes=8),
+                                    dict(block_threads=64, staged_threads=64),
+                                    dict(refill_lanes=1), dict(refill_lanes=32, block_threads=256)])
 def test_staged_tuning_invariance(ctx, tuning):
     import treelet_rt as rt
 

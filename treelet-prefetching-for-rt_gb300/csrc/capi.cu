@@ -114,7 +114,8 @@ struct rt_scene {
   // per-launch counters and status (library scratch)
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
-  rt_tuning tuning{128, 256, 16, 4};
+  uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
+  rt_tuning tuning{128, 128, 4, 1, 8, 0, 2};
   // host-buffer path scratch
   cudaStream_t stream = nullptr;
   void* d_io = nullptr;
@@ -159,6 +160,18 @@ void free_treelets(rt_scene* s) {
   s->d_member_first = nullptr;
   s->d_member_bytes = nullptr;
   s->has_treelets = false;
+}
+
+// Blocks for a persistent launch: as many as fit on the device at once (no
+// more than the rays need).
+uint32_t persistent_grid(const void* kern, uint32_t threads, uint32_t n, size_t dyn_smem = 0) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)threads, dyn_smem);
+  const uint64_t full = (uint64_t)std::max(1, sms) * (uint64_t)std::max(1, per_sm);
+  const uint64_t need = ((uint64_t)n + threads - 1) / threads;
+  return (uint32_t)std::max<uint64_t>(1, std::min(full, need));
 }
 
 int max_smem_per_block() {
@@ -215,6 +228,7 @@ rt_status rt_scene_create(rt_ctx* ctx, const rt_blob* blob, rt_scene** out) {
   rt_status st = dalloc(&s->d_blob, s->blob_bytes);
   if (st == RT_OK) st = dalloc(&s->d_stats, sizeof(unsigned long long) * rtk::ST_COUNT);
   if (st == RT_OK) st = dalloc(&s->d_status, sizeof(uint32_t));
+  if (st == RT_OK) st = dalloc(&s->d_queue, sizeof(uint32_t));
   if (st != RT_OK) {
     rt_scene_destroy(s);
     return st;
@@ -238,6 +252,7 @@ rt_status rt_scene_destroy(rt_scene* s) {
   cudaFree(s->d_blob);
   cudaFree(s->d_stats);
   cudaFree(s->d_status);
+  cudaFree(s->d_queue);
   cudaFree(s->d_io);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -334,9 +349,22 @@ rt_status rt_scene_set_tuning(rt_scene* s, const rt_tuning* t) {
     n.staged_threads = t->staged_threads;
   }
   if (t->staged_epoch) n.staged_epoch = t->staged_epoch;
+  if (t->refill_lanes) {
+    if (t->refill_lanes > 32) return rti::fail(RT_ERR_INVALID, "refill_lanes must be 1..32");
+    n.refill_lanes = t->refill_lanes;
+  }
   if (t->staged_slots) {
-    if (t->staged_slots > (uint32_t)rtk::kMaxSlots) return rti::fail(RT_ERR_INVALID, "staged_slots above 32");
+    if (t->staged_slots > (uint32_t)rtk::kMaxSlots) return rti::fail(RT_ERR_INVALID, "staged_slots must be 1..8");
     n.staged_slots = t->staged_slots;
+  }
+  if (t->staged_slot_bytes) {
+    if (t->staged_slot_bytes < 64 || t->staged_slot_bytes > 65536)
+      return rti::fail(RT_ERR_INVALID, "staged_slot_bytes must be 64..65536");
+    n.staged_slot_bytes = t->staged_slot_bytes;
+  }
+  if (t->staged_min_votes) {
+    if (t->staged_min_votes > 32) return rti::fail(RT_ERR_INVALID, "staged_min_votes must be 1..32");
+    n.staged_min_votes = t->staged_min_votes;
   }
   s->tuning = n;
   return RT_OK;
@@ -379,27 +407,37 @@ rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint3
   a.stats = s->d_stats;
   a.status = s->d_status;
   a.epoch = s->tuning.staged_epoch;
+  a.queue = s->d_queue;
+  a.refill = s->tuning.refill_lanes;
   RT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, st));
   RT_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), st));
+  RT_CUDA(cudaMemsetAsync(s->d_queue, 0, sizeof(uint32_t), st));
   if (mode == RT_MODE_PLAIN) {
     const uint32_t bt = s->tuning.block_threads;
-    rtk::trace_plain_kernel<kPlainCap><<<(n + bt - 1) / bt, bt, 0, st>>>(a);
+    auto kern = rtk::trace_plain_kernel<kPlainCap>;
+    kern<<<persistent_grid((const void*)kern, bt, n), bt, 0, st>>>(a);
   } else if (mode == RT_MODE_TREELET) {
     const uint32_t bt = s->tuning.block_threads;
-    rtk::trace_treelet_kernel<kTreeletCap><<<(n + bt - 1) / bt, bt, 0, st>>>(a);
+    auto kern = rtk::trace_treelet_kernel<kTreeletCap>;
+    kern<<<persistent_grid((const void*)kern, bt, n), bt, 0, st>>>(a);
   } else {
     if (s->part.roots.size() >= rtt::kMaxDense)
       return rti::fail(RT_ERR_TOO_LARGE, "rt_trace: too many treelets for staged mode (max 4194304)");
     const uint32_t bt = s->tuning.staged_threads;
+    const uint32_t warps = bt / 32;
+    // per-warp slots: the whole largest image, or the first staged_slot_bytes of each
+    uint32_t slot_bytes = s->slot_bytes;
+    if (s->tuning.staged_slot_bytes) slot_bytes = std::min(slot_bytes, (s->tuning.staged_slot_bytes + 127u) & ~127u);
     uint32_t slots = s->tuning.staged_slots;
-    const int limit = max_smem_per_block() - (int)sizeof(rtk::StagedShared) - 1024;
-    while (slots > 0 && (int)(slots * s->slot_bytes + 128) > limit) --slots;
+    const int limit = max_smem_per_block() - (int)(sizeof(rtk::WarpStage) * 8) - 1024;
+    while (slots > 0 && (int)(warps * slots * slot_bytes + 128) > limit) --slots;
     a.slots = slots;
-    a.slot_bytes = s->slot_bytes;
-    const size_t dyn = (size_t)slots * s->slot_bytes + 128;
+    a.slot_bytes = slot_bytes;
+    a.min_votes = s->tuning.staged_min_votes;
+    const size_t dyn = (size_t)warps * slots * slot_bytes + 128;
     auto kern = rtk::trace_staged_kernel<kTreeletCap>;
     RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-    kern<<<(n + bt - 1) / bt, bt, dyn, st>>>(a);
+    kern<<<persistent_grid((const void*)kern, bt, n, dyn), bt, dyn, st>>>(a);
   }
   RT_CUDA(cudaGetLastError());
   return RT_OK;

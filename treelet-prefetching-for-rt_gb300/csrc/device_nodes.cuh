@@ -50,9 +50,35 @@ struct ChildHits {
   __device__ __forceinline__ uint32_t info_of(int i) const { return (uint32_t)(info >> (8 * i)) & 0x3fu; }
 };
 
+// Byte b of the node as an exact float: the byte is placed in the mantissa of
+// 2^23 with one byte permute, and 2^23 subtracted (both steps exact).
+__device__ __forceinline__ float byte_as_float(const Node64& n, int b) {
+  const uint32_t sel = (uint32_t)(b & 3) | 0x7540u;  // bytes: q, 0x00, 0x00, 0x4B
+  return __uint_as_float(__byte_perm(n.w[b >> 2], 0x4B000000u, sel)) - 8388608.0f;
+}
+
+// The six-way min/max of the slab test.  EXACT uses the reference's ternary
+// MIN/MAX macros.  FAST uses fminf/fmaxf, which agree with the ternaries
+// except on NaN operands and on the sign of a zero result; with a finite ray
+// origin and direction no slab value is NaN, and the sign of thit's zero
+// never changes a comparison, so both give the same hit / cull decisions.
+template <bool FAST>
+__device__ __forceinline__ float mn2(float a, float b) {
+  if (FAST) return fminf(a, b);
+  return rtm::tmin2(a, b);
+}
+template <bool FAST>
+__device__ __forceinline__ float mx2(float a, float b) {
+  if (FAST) return fmaxf(a, b);
+  return rtm::tmax2(a, b);
+}
+
 // The box tests of an internal node (vulkan_ray_tracing.cc:2518-2553 and the
 // bottom-level twin :2714-2741): children with ChildSize > 0 are slab-tested
-// with the ray's [tmin, tmax]; a hit at thit >= cull is dropped.
+// with the ray's [tmin, tmax]; a hit at thit >= cull is dropped.  Bounds are
+// Origin + ldexpf(q, exp - 8) (asu.h:499-508), slab values (b - o) * idir
+// (vulkan_ray_tracing.cc:199-218), reduced as magic_max7 / magic_min7.
+template <bool FAST>
 __device__ __forceinline__ ChildHits test_children(const Node64& n, uint32_t node_unit, rtm::V3 o, rtm::V3 idir,
                                                    float tmin, float tmax, float cull) {
   ChildHits r;
@@ -61,27 +87,37 @@ __device__ __forceinline__ ChildHits test_children(const Node64& n, uint32_t nod
   const int ex = (int)(int8_t)byte_at(n, 18), ey = (int)(int8_t)byte_at(n, 19), ez = (int)(int8_t)byte_at(n, 20);
   const float sx = rtm::exp2_int(ex - 8), sy = rtm::exp2_int(ey - 8), sz = rtm::exp2_int(ez - 8);
   r.hit_mask = 0;
-  r.info = 0;
+  r.info = ((uint64_t)n.w[6] << 16) | (n.w[5] >> 16);  // bytes 22..27
+  r.info &= 0x3f3f3f3f3f3full;
   r.child_unit = (uint32_t)((int)node_unit + child_off);
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    const uint32_t info = byte_at(n, 22 + i) & 0x3fu;
-    r.info |= (uint64_t)info << (8 * i);
+    const uint32_t info = r.info_of(i);
     if (info & 3u) {
-      rtm::V3 lo, hi;
-      lo.x = ox + (float)byte_at(n, rtf::IN_LO_X + i) * sx;
-      lo.y = oy + (float)byte_at(n, rtf::IN_LO_Y + i) * sy;
-      lo.z = oz + (float)byte_at(n, rtf::IN_LO_Z + i) * sz;
-      hi.x = ox + (float)byte_at(n, rtf::IN_HI_X + i) * sx;
-      hi.y = oy + (float)byte_at(n, rtf::IN_HI_Y + i) * sy;
-      hi.z = oz + (float)byte_at(n, rtf::IN_HI_Z + i) * sz;
-      float thit;
-      bool h = rtm::ray_box_test(lo, hi, idir, o, tmin, tmax, thit);
-      if (h && thit >= cull) h = false;
+      const float lx = ((ox + byte_as_float(n, rtf::IN_LO_X + i) * sx) - o.x) * idir.x;
+      const float ly = ((oy + byte_as_float(n, rtf::IN_LO_Y + i) * sy) - o.y) * idir.y;
+      const float lz = ((oz + byte_as_float(n, rtf::IN_LO_Z + i) * sz) - o.z) * idir.z;
+      const float hx = ((ox + byte_as_float(n, rtf::IN_HI_X + i) * sx) - o.x) * idir.x;
+      const float hy = ((oy + byte_as_float(n, rtf::IN_HI_Y + i) * sy) - o.y) * idir.y;
+      const float hz = ((oz + byte_as_float(n, rtf::IN_HI_Z + i) * sz) - o.z) * idir.z;
+      const float t1 = mx2<FAST>(mn2<FAST>(lx, hx), tmin);
+      const float t2 = mx2<FAST>(mn2<FAST>(ly, hy), t1);
+      const float tn = mx2<FAST>(mn2<FAST>(lz, hz), t2);
+      const float u1 = mn2<FAST>(mx2<FAST>(lx, hx), tmax);
+      const float u2 = mn2<FAST>(mx2<FAST>(ly, hy), u1);
+      const float tf = mn2<FAST>(mx2<FAST>(lz, hz), u2);
+      bool h = tn <= tf;
+      if (h && tn >= cull) h = false;
       if (h) r.hit_mask |= 1u << i;
     }
   }
   return r;
+}
+
+// True when the slab test may use the FAST min/max (see mn2).
+__device__ __forceinline__ bool finite_ray(rtm::V3 o, rtm::V3 d, float tmin, float tmax) {
+  return isfinite(o.x) && isfinite(o.y) && isfinite(o.z) && isfinite(d.x) && isfinite(d.y) && isfinite(d.z) &&
+         !isnan(tmin) && !isnan(tmax);
 }
 
 // Instance leaf fields used by the walk.

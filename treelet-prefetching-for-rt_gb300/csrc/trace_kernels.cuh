@@ -53,6 +53,9 @@ struct TraceArgs {
   uint32_t slots;              // staged treelet slots per CTA
   uint32_t slot_bytes;         // bytes per slot (multiple of 128)
   uint32_t epoch;              // node visits per ray between votes
+  uint32_t* queue;             // next ray to hand out (persistent kernels; zeroed per launch)
+  uint32_t refill;             // idle lanes of a warp that trigger a refill
+  uint32_t min_votes;          // lanes that must want a treelet before a warp stages it
 };
 
 struct Recorder {
@@ -153,155 +156,232 @@ __device__ __forceinline__ void add_warp_total(unsigned long long* dst, uint32_t
   if ((threadIdx.x & 31u) == (uint32_t)(__ffs(mask) - 1)) atomicAdd(dst, (unsigned long long)sum);
 }
 
-// ----------------------------------------------------------------- plain
-template <int CAP>
-__global__ void __launch_bounds__(256) trace_plain_kernel(TraceArgs a) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.n) return;
-  rtm::V3 O, D;
-  float tmin, tmax;
-  load_ray(a.rays, r, O, tmin, D, tmax);
-  const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
-  const bool terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
-  const bool opaque = flags & rtf::RAY_FLAG_OPAQUE;
-  Recorder rec{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
-               a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, a.meta};
-  uint32_t status = 0;
-  uint32_t stk[CAP];
-  int sp = 0;
-  float min_thit = tmax;
-  uint32_t c_leaf = 0, c_inst = 0;
-  float c_tobj = 0.0f;
-  const rtm::V3 idir = rtm::calculate_idir(D);
+// The same for 64-bit values; all 32 lanes must call it.
+__device__ __forceinline__ void add_warp_total64(unsigned long long* dst, unsigned long long v) {
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+  if ((threadIdx.x & 31u) == 0) atomicAdd(dst, v);
+}
 
-  rec.rec(0, rtf::TX_STRUCTURE);
-  {
+// Finds a ray for every idle lane of the warp (one atomic per refill) and
+// runs each lane's walker one node visit per iteration.  A lane that finishes
+// its ray gets a new one as soon as `refill` lanes of its warp are idle, so
+// warps stay full while rays of very different lengths finish (persistent
+// threads with dynamic ray fetch).  Every ray's own visit order is unchanged.
+template <class W>
+__device__ __forceinline__ void run_persistent(const TraceArgs& a, W& w, unsigned long long& bytes_out) {
+  const uint32_t lane = threadIdx.x & 31u;
+  bool have = false, exhausted = false;
+  uint32_t r = 0;
+  unsigned long long bytes = 0;
+  for (;;) {
+    const uint32_t need = __ballot_sync(0xffffffffu, !have);
+    if (!exhausted && need && (__popc(need) >= (int)a.refill || need == 0xffffffffu)) {
+      const int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(a.queue, (uint32_t)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (uint32_t)__popc(need) >= a.n) exhausted = true;
+      if (!have) {
+        const uint32_t rr = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
+        if (rr < a.n) {
+          r = rr;
+          w.init(a, r);
+          have = true;
+          if (!w.active()) {
+            w.finish(a, r);
+            bytes += w.rec.bytes;
+            have = false;
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, have)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (have) {
+      w.step(a);
+      if (!w.active()) {
+        w.finish(a, r);
+        bytes += w.rec.bytes;
+        have = false;
+      }
+    }
+  }
+  bytes_out = bytes;
+}
+
+// ----------------------------------------------------------------- plain
+
+// A ray's traceRay walk (vulkan_ray_tracing.cc:2309-3076) as a sequence of
+// node visits.  One LIFO stack of unit << 2 | top | leaf entries; `next` is
+// the internal node descended next (the first hit internal child, :2570-2578);
+// leaves and further children are pushed.  A top-level instance leaf is
+// followed by its whole BLAS before the next top-level entry (:2602-2679).
+template <int CAP>
+struct PlainWalker {
+  rtm::V3 O, D, idir;
+  float tmin, tmax, min_thit, c_tobj;
+  bool opaque, terminate, inblas, fast;
+  uint32_t next, c_leaf, c_inst, status;
+  int sp;
+  uint32_t stk[CAP];
+  InstCtx ic;
+  bool ic_fast;
+  Recorder rec;
+
+  __device__ __forceinline__ bool active() const { return next != kNone || sp > 0; }
+
+  __device__ __forceinline__ void push(uint32_t e) {
+    if (sp < CAP) stk[sp++] = e;
+    else status |= RT_RAY_STACK_OVERFLOW;
+  }
+
+  __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
+    load_ray(a.rays, r, O, tmin, D, tmax);
+    const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
+    terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
+    opaque = flags & rtf::RAY_FLAG_OPAQUE;
+    rec = Recorder{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
+                   a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, a.meta};
+    status = 0;
+    sp = 0;
+    next = kNone;
+    inblas = false;
+    min_thit = tmax;
+    c_leaf = c_inst = 0;
+    c_tobj = 0.0f;
+    ic.unit = kNone;
+    ic_fast = false;
+    idir = rtm::calculate_idir(D);
+    fast = rtd::finite_ray(O, D, tmin, tmax);
+    rec.rec(0, rtf::TX_STRUCTURE);
     const uint4 h0 = __ldg(a.blob), h1 = __ldg(a.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
     const rtm::V3 bmax = rtm::v3(__uint_as_float(h1.y), __uint_as_float(h1.z), __uint_as_float(h1.w));
     float th;
-    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) stk[sp++] = ((uint32_t)(root_off >> 6) << 2) | kTop;
+    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) push(((uint32_t)(root_off >> 6) << 2) | kTop);
   }
-  uint32_t next = kNone;
-  bool inblas = false;
-  InstCtx ic;
-  ic.unit = kNone;
-  for (;;) {
-    if (next != kNone) {
-      const uint32_t unit = next;
-      if (unit >= a.n_units) {
-        status |= RT_RAY_BAD_NODE;
-        break;
-      }
-      rec.rec(unit, rtf::TX_INTERNAL);
-      rtd::Node64 nd;
-      rtd::load64(a.blob + (uint64_t)unit * 4, 0, nd);
-      const rtd::ChildHits ch = inblas ? rtd::test_children(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, min_thit * ic.mult)
-                                       : rtd::test_children(nd, unit, O, idir, tmin, tmax, min_thit);
-      const uint32_t level = inblas ? 0u : kTop;
-      uint32_t c = ch.child_unit;
-      uint32_t nn = kNone;
-#pragma unroll
-      for (int i = 0; i < 6; ++i) {
-        const uint32_t info = ch.info_of(i);
-        if ((ch.hit_mask >> i) & 1u) {
-          if ((info >> 2) != rtf::CT_INTERNAL) {
-            if (sp < CAP) stk[sp++] = (c << 2) | level | kLeaf;
-            else status |= RT_RAY_STACK_OVERFLOW;
-          } else if (nn == kNone) {
-            nn = c;
-          } else {
-            if (sp < CAP) stk[sp++] = (c << 2) | level;
-            else status |= RT_RAY_STACK_OVERFLOW;
-          }
-        }
-        c += info & 3u;
-      }
-      if (status & RT_RAY_STACK_OVERFLOW) break;
-      next = nn;
-      continue;
-    }
+
+  __device__ __forceinline__ void stop(uint32_t bits) {
+    status |= bits;
+    sp = 0;
+    next = kNone;
+  }
+
+  __device__ __forceinline__ void visit_internal(const TraceArgs& a, uint32_t unit) {
+    if (unit >= a.n_units) return stop(RT_RAY_BAD_NODE);
+    rec.rec(unit, rtf::TX_INTERNAL);
+    rtd::Node64 nd;
+    rtd::load64(a.blob + (uint64_t)unit * 4, 0, nd);
+    rtd::ChildHits ch;
     if (inblas) {
-      if (sp > 0 && !(stk[sp - 1] & kTop)) {
-        const uint32_t e = stk[--sp];
-        const uint32_t unit = e >> 2;
-        if (!(e & kLeaf)) {
-          next = unit;
-          continue;
-        }
-        if (unit >= a.n_units) {
-          status |= RT_RAY_BAD_NODE;
-          break;
-        }
-        rec.rec(unit, rtf::TX_LEAF_DESC);
-        rtd::Node64 q;
-        rtd::load64(a.blob + (uint64_t)unit * 4, 0, q);
-        if (rtf::leaf_type_of(q.w[1]) == 0) {
-          const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
-          const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
-          const rtm::V3 v2 = rtm::v3(__uint_as_float(q.w[10]), __uint_as_float(q.w[11]), __uint_as_float(q.w[12]));
-          float t = 0.0f;
-          const bool hit = rtm::ray_triangle_test(v0, v1, v2, ic.o, ic.d, t);
-          const float wt = t / ic.mult;
-          if (hit && tmin <= wt && wt <= tmax) {
-            if (opaque && wt < min_thit) min_thit = t / ic.mult;
-            c_leaf = unit;
-            c_inst = ic.unit;
-            c_tobj = t;
-            rec.rec(unit, rtf::TX_QUAD_LEAF_HIT);
-            if (terminate) sp = 0;
-          } else {
-            rec.rec(unit, rtf::TX_QUAD_LEAF);
-          }
-        } else {
-          status |= RT_RAY_HIT_PROCEDURAL;
-          rec.rec(unit, rtf::TX_PROCEDURAL_LEAF);
-        }
-        continue;
+      const float cull = min_thit * ic.mult;
+      ch = ic_fast ? rtd::test_children<true>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull)
+                   : rtd::test_children<false>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull);
+    } else {
+      ch = fast ? rtd::test_children<true>(nd, unit, O, idir, tmin, tmax, min_thit)
+                : rtd::test_children<false>(nd, unit, O, idir, tmin, tmax, min_thit);
+    }
+    const uint32_t level = inblas ? 0u : kTop;
+    uint32_t c = ch.child_unit, nn = kNone;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const uint32_t info = ch.info_of(i);
+      if ((ch.hit_mask >> i) & 1u) {
+        if ((info >> 2) != rtf::CT_INTERNAL) push((c << 2) | level | kLeaf);
+        else if (nn == kNone) nn = c;
+        else push((c << 2) | level);
       }
-      inblas = false;
-      continue;
+      c += info & 3u;
     }
-    if (sp == 0) break;
-    const uint32_t e = stk[--sp];
-    const uint32_t unit = e >> 2;
-    if (!(e & kLeaf)) {
-      next = unit;
-      continue;
+    next = nn;
+    if (status & RT_RAY_STACK_OVERFLOW) stop(0);
+  }
+
+  __device__ __forceinline__ void visit_leaf(const TraceArgs& a, uint32_t unit) {
+    if (unit >= a.n_units) return stop(RT_RAY_BAD_NODE);
+    rec.rec(unit, rtf::TX_LEAF_DESC);
+    rtd::Node64 q;
+    rtd::load64(a.blob + (uint64_t)unit * 4, 0, q);
+    if (rtf::leaf_type_of(q.w[1]) == 0) {
+      const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
+      const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
+      const rtm::V3 v2 = rtm::v3(__uint_as_float(q.w[10]), __uint_as_float(q.w[11]), __uint_as_float(q.w[12]));
+      float t = 0.0f;
+      const bool hit = rtm::ray_triangle_test(v0, v1, v2, ic.o, ic.d, t);
+      const float wt = t / ic.mult;
+      if (hit && tmin <= wt && wt <= tmax) {  // :2843-2859
+        if (opaque && wt < min_thit) min_thit = t / ic.mult;
+        c_leaf = unit;
+        c_inst = ic.unit;
+        c_tobj = t;
+        rec.rec(unit, rtf::TX_QUAD_LEAF_HIT);
+        if (terminate) sp = 0;
+      } else {
+        rec.rec(unit, rtf::TX_QUAD_LEAF);
+      }
+    } else {
+      status |= RT_RAY_HIT_PROCEDURAL;
+      rec.rec(unit, rtf::TX_PROCEDURAL_LEAF);
     }
-    // instance leaf (vulkan_ray_tracing.cc:2602-2676)
-    if (unit + 1 >= a.n_units) {
-      status |= RT_RAY_BAD_NODE;
-      break;
-    }
+  }
+
+  __device__ __forceinline__ void visit_instance(const TraceArgs& a, uint32_t unit) {
+    if (unit + 1 >= a.n_units) return stop(RT_RAY_BAD_NODE);
     rec.rec(unit, rtf::TX_INSTANCE_LEAF);
     rtd::Instance in;
     rtd::load_instance(a.blob + (uint64_t)unit * 4, 0, in);
     const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
-    if ((hdr & 63) || hdr / 64 >= a.n_units) {
-      status |= RT_RAY_BAD_NODE;
-      break;
-    }
+    if ((hdr & 63) || hdr / 64 >= a.n_units) return stop(RT_RAY_BAD_NODE);
     rec.rec((uint32_t)(hdr >> 6), rtf::TX_STRUCTURE);
     const uint4 h0 = __ldg(a.blob + (hdr >> 4));
     const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
     enter_instance(in, unit, O, D, tmin, tmax, ic);
-    if (sp < CAP) {
-      stk[sp++] = (uint32_t)(broot >> 6) << 2;
-    } else {
-      status |= RT_RAY_STACK_OVERFLOW;
-      break;
-    }
+    ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
+    push((uint32_t)(broot >> 6) << 2);
     inblas = true;
+    if (status & RT_RAY_STACK_OVERFLOW) stop(0);
   }
-  const bool hit = min_thit < tmax;
-  if (status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE)) {
-    write_hit(a, r, false, min_thit, O, D, tmin, tmax, 0, 0, 0.0f, rec, status);
-  } else {
-    write_hit(a, r, hit, min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
+
+  // One node visit (the caller checks active() first).
+  __device__ __forceinline__ void step(const TraceArgs& a) {
+    for (;;) {
+      if (next != kNone) return visit_internal(a, next);
+      if (inblas) {
+        if (sp > 0 && !(stk[sp - 1] & kTop)) {
+          const uint32_t e = stk[--sp];
+          if (e & kLeaf) return visit_leaf(a, e >> 2);
+          next = e >> 2;
+          continue;
+        }
+        inblas = false;
+        continue;
+      }
+      if (sp == 0) return;
+      const uint32_t e = stk[--sp];
+      if (!(e & kLeaf)) {
+        next = e >> 2;
+        continue;
+      }
+      return visit_instance(a, e >> 2);
+    }
   }
-  if (a.stats) add_warp_total(a.stats + ST_NODE_BYTES, rec.bytes);
+
+  __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
+    const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);
+    write_hit(a, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
+  }
+};
+
+template <int CAP>
+__global__ void __launch_bounds__(256) trace_plain_kernel(TraceArgs a) {
+  PlainWalker<CAP> w;
+  unsigned long long bytes = 0;
+  run_persistent(a, w, bytes);
+  if (a.stats) add_warp_total64(a.stats + ST_NODE_BYTES, bytes);
 }
 
 }  // namespace rtk

@@ -1,5 +1,5 @@
 // Treelet-ordered traversal (traceRayWithTreelets, vulkan_ray_tracing.cc:1522-2307)
-// with optional shared-memory staging of treelets.
+// and its shared-memory staged variant.
 #pragma once
 #include "trace_kernels.cuh"
 
@@ -8,50 +8,60 @@ namespace rtk {
 constexpr uint32_t kSlotBitsDev = 10;
 
 // A ray's treelet-ordered walk.  Two LIFO stacks as in the reference
-// (push_front / pop_front on std::list): `cur` for nodes in the current
-// treelet, `oth` for the rest.  An entry carries the node (unit << 2 | top |
-// leaf), the instance leaf it belongs to (bottom-level entries) and the
-// node's staged location.
-template <int CAP>
+// (push_front / pop_front on std::list, :1708-1709): `cur` holds nodes of the
+// current treelet, `oth` the rest (:1821-1856).  An entry packs the node
+// (unit << 2 | top | leaf) and, for bottom-level nodes, the instance leaf it
+// belongs to; with STAGED it also keeps the node's staged location
+// (dense treelet << 10 | 64-byte slot in that treelet's image).
+template <int CAP, bool STAGED>
 struct Walker {
   rtm::V3 O, D, idir;
   float tmin, tmax, min_thit, c_tobj;
-  bool terminate;
+  bool terminate, fast, ic_fast;  // FAST min/max allowed for the world / object ray
   uint32_t c_leaf, c_inst, current_root, status;
   int cn, on;
-  uint32_t cu_code[CAP], cu_inst[CAP], cu_loc[CAP];
-  uint32_t ot_code[CAP], ot_inst[CAP], ot_loc[CAP];
+  unsigned long long cu[CAP], ot[CAP];
+  uint32_t cu_loc[STAGED ? CAP : 1], ot_loc[STAGED ? CAP : 1];
   InstCtx ic;
   Recorder rec;
   uint32_t smem_reads, gmem_reads;
 
   __device__ __forceinline__ bool active() const { return cn > 0 || on > 0; }
 
-  // Unit index of the node the ray visits next (its first pending access).
+  // Staged location of the node the ray visits next (its first pending access).
   __device__ __forceinline__ uint32_t next_loc() const {
+    if (!STAGED) return kNone;
     if (cn > 0) return cu_loc[cn - 1];
     if (on > 0) return ot_loc[on - 1];
     return kNone;
   }
 
+  // addrToTreeletID(child) == current_treelet_root ? current : other.
   __device__ __forceinline__ void route(const TraceArgs& a, uint32_t code, uint32_t inst) {
     const uint32_t unit = code >> 2;
-    uint2 m = make_uint2(kNone, kNone);
-    if (unit < a.n_units) m = __ldg(a.meta + unit);
-    if (m.x == current_root) {
+    uint32_t root = kNone, loc = kNone;
+    if (unit < a.n_units) {
+      if (STAGED) {
+        const uint2 m = __ldg(a.meta + unit);
+        root = m.x;
+        loc = m.y;
+      } else {
+        root = __ldg(reinterpret_cast<const uint32_t*>(a.meta) + 2ull * unit);
+      }
+    }
+    const unsigned long long e = (unsigned long long)code | ((unsigned long long)inst << 32);
+    if (root == current_root) {
       if (cn < CAP) {
-        cu_code[cn] = code;
-        cu_inst[cn] = inst;
-        cu_loc[cn] = m.y;
+        cu[cn] = e;
+        if (STAGED) cu_loc[cn] = loc;
         ++cn;
       } else {
         status |= RT_RAY_STACK_OVERFLOW;
       }
     } else {
       if (on < CAP) {
-        ot_code[on] = code;
-        ot_inst[on] = inst;
-        ot_loc[on] = m.y;
+        ot[on] = e;
+        if (STAGED) ot_loc[on] = loc;
         ++on;
       } else {
         status |= RT_RAY_STACK_OVERFLOW;
@@ -74,6 +84,8 @@ struct Walker {
     ic.unit = kNone;
     smem_reads = gmem_reads = 0;
     idir = rtm::calculate_idir(D);
+    fast = rtd::finite_ray(O, D, tmin, tmax);
+    ic_fast = false;
     rec.rec(0, rtf::TX_STRUCTURE);
     const uint4 h0 = __ldg(a.blob), h1 = __ldg(a.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
@@ -88,24 +100,26 @@ struct Walker {
     rtd::Instance in;
     rtd::load_instance(a.blob + (uint64_t)inst * 4, 0, in);
     enter_instance(in, inst, O, D, tmin, tmax, ic);
+    ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
   }
 
-  // Visits one node.  `saddr` is its shared-memory address when staged, else 0.
+  // Visits one node; `lookup(loc)` returns its shared-memory address when it
+  // is staged, else 0.
   template <class Lookup>
   __device__ __forceinline__ void step(const TraceArgs& a, Lookup&& lookup) {
-    uint32_t code, inst, loc;
+    unsigned long long e;
+    uint32_t loc = kNone;
     if (cn == 0) {  // :1748-1754
       --on;
-      code = ot_code[on];
-      inst = ot_inst[on];
-      loc = ot_loc[on];
-      current_root = code >> 2;
+      e = ot[on];
+      if (STAGED) loc = ot_loc[on];
+      current_root = (uint32_t)e >> 2;
     } else {
       --cn;
-      code = cu_code[cn];
-      inst = cu_inst[cn];
-      loc = cu_loc[cn];
+      e = cu[cn];
+      if (STAGED) loc = cu_loc[cn];
     }
+    const uint32_t code = (uint32_t)e, inst = (uint32_t)(e >> 32);
     const uint32_t unit = code >> 2;
     const bool top = code & kTop, leaf = code & kLeaf;
     if (unit + ((top && leaf) ? 1u : 0u) >= a.n_units) {
@@ -113,9 +127,12 @@ struct Walker {
       cn = on = 0;
       return;
     }
-    const uint32_t saddr = lookup(loc);
-    if (saddr) ++smem_reads;
-    else ++gmem_reads;
+    uint32_t saddr = 0;
+    if (STAGED) {
+      saddr = lookup(loc);
+      if (saddr) ++smem_reads;
+      else ++gmem_reads;
+    }
     const uint4* g = a.blob + (uint64_t)unit * 4;
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
       rec.rec(unit, rtf::TX_INTERNAL);
@@ -123,10 +140,13 @@ struct Walker {
       rtd::load64(g, saddr, nd);
       rtd::ChildHits ch;
       if (top) {
-        ch = rtd::test_children(nd, unit, O, idir, tmin, tmax, min_thit);
+        ch = fast ? rtd::test_children<true>(nd, unit, O, idir, tmin, tmax, min_thit)
+                  : rtd::test_children<false>(nd, unit, O, idir, tmin, tmax, min_thit);
       } else {
         ensure_instance(a, inst);
-        ch = rtd::test_children(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, min_thit * ic.mult);
+        const float cull = min_thit * ic.mult;
+        ch = ic_fast ? rtd::test_children<true>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull)
+                     : rtd::test_children<false>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull);
       }
       const uint32_t level = top ? kTop : 0u;
       uint32_t c = ch.child_unit;
@@ -153,6 +173,7 @@ struct Walker {
       const uint4 h0 = __ldg(a.blob + (hdr >> 4));
       const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
       enter_instance(in, unit, O, D, tmin, tmax, ic);
+      ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
       route(a, (uint32_t)(broot >> 6) << 2, unit);
     } else {  // primitive leaf (:2071-2196)
       rec.rec(unit, rtf::TX_LEAF_DESC);
@@ -166,7 +187,7 @@ struct Walker {
         float t = 0.0f;
         const bool hit = rtm::ray_triangle_test(v0, v1, v2, ic.o, ic.d, t);
         const float wt = t / ic.mult;
-        if (hit && tmin <= wt && wt <= tmax && wt < min_thit) {
+        if (hit && tmin <= wt && wt <= tmax && wt < min_thit) {  // :2127-2141
           min_thit = t / ic.mult;
           c_tobj = t;
           c_leaf = unit;
@@ -184,6 +205,10 @@ struct Walker {
     if (status & RT_RAY_STACK_OVERFLOW) cn = on = 0;
   }
 
+  __device__ __forceinline__ void step(const TraceArgs& a) {
+    step(a, [](uint32_t) -> uint32_t { return 0u; });
+  }
+
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
     const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);
     write_hit(a, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
@@ -192,14 +217,10 @@ struct Walker {
 
 template <int CAP>
 __global__ void __launch_bounds__(256) trace_treelet_kernel(TraceArgs a) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.n) return;
-  Walker<CAP> w;
-  w.init(a, r);
-  auto no_stage = [](uint32_t) -> uint32_t { return 0u; };
-  while (w.active()) w.step(a, no_stage);
-  w.finish(a, r);
-  if (a.stats) add_warp_total(a.stats + ST_NODE_BYTES, w.rec.bytes);
+  Walker<CAP, false> w;
+  unsigned long long bytes = 0;
+  run_persistent(a, w, bytes);
+  if (a.stats) add_warp_total64(a.stats + ST_NODE_BYTES, bytes);
 }
 
 // ------------------------------------------------------------------ staged
@@ -213,6 +234,17 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// One non-blocking probe of the phase with the given parity.
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
 }
 
 // Bounded wait for the phase with the given parity; false if it gave up.
@@ -230,6 +262,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 
+// Global -> shared bulk copy completing on `bar`.  The fence orders this
+// thread's earlier generic-proxy accesses before the async-proxy writes.
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile(
@@ -238,152 +272,160 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
       : "memory");
 }
 
-constexpr int kHashSize = 512;   // vote table entries (>= 2 x threads per CTA)
-constexpr int kMaxSlots = 32;
+constexpr int kMaxSlots = 8;  // slots per warp
 constexpr uint32_t kWaitTries = 1u << 22;
 
-struct StagedShared {
+// Per-warp staging state in shared memory.
+struct WarpStage {
   uint64_t bar;
   uint32_t resident[kMaxSlots];  // dense treelet id per slot, or kNone
-  uint32_t pending_slot, pending_id, phase, disabled, victim;
-  uint32_t hkey[kHashSize];
-  uint32_t hcnt[kHashSize];
-  unsigned long long best[8];
-  unsigned long long staged_bytes, stagings;
+  uint32_t units[kMaxSlots];     // 64-byte units of that treelet held in the slot
+  uint32_t pending_slot, pending_id, pending_units, phase, victim, disabled;
 };
 
-// One CTA = the rays of one RT unit.  Each epoch: finish the previous copy,
-// vote on the treelet the most rays access next, start copying it into a
-// slot, then let every ray walk up to `epoch` nodes.
+// The staged walk.  Persistent warps with ray refill (as run_persistent).
+// Every `epoch` node visits a warp votes: each lane names the treelet of its
+// next access, __match_any_sync counts equal names, and the most popular
+// treelet that is not resident (ties to the lowest treelet, i.e. the lowest
+// root address, as the RT unit's decision in shader.cc:3424-3441) is copied
+// with cp.async.bulk into the warp's least recently filled slot, provided at
+// least `min_votes` lanes want it.  A slot holds the first slot_bytes of the
+// treelet's image (the whole image when it fits).  Node reads that fall in a
+// resident slot are served from shared memory.  A slot is read only by its
+// own warp; __syncwarp orders the slot's reads before it is refilled.
 template <int CAP>
 __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
   extern __shared__ __align__(128) uint8_t dyn_smem[];
-  __shared__ StagedShared sh;
-  // slots start on a 128-byte boundary (the launch adds 128 bytes of room)
-  uint8_t* const slot_mem = dyn_smem + ((128u - (smem_u32(dyn_smem) & 127u)) & 127u);
-  const uint32_t tid = threadIdx.x;
-  const uint32_t r = blockIdx.x * blockDim.x + tid;
-  const bool mine = r < a.n;
-  Walker<CAP> w;
-  if (mine) w.init(a, r);
-  else w.cn = w.on = 0;
+  __shared__ WarpStage ws[8];
+  uint8_t* const smem0 = dyn_smem + ((128u - (smem_u32(dyn_smem) & 127u)) & 127u);
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t slots = a.slots;
-  if (tid == 0) {
-    mbar_init(&sh.bar, 1);
-    sh.pending_slot = kNone;
-    sh.pending_id = kNone;
-    sh.phase = 0;
-    sh.disabled = 0;
-    sh.victim = 0;
-    sh.staged_bytes = 0;
-    sh.stagings = 0;
+  uint8_t* const my_slots = smem0 + (size_t)warp * slots * a.slot_bytes;
+  const uint32_t slot_base = smem_u32(my_slots);
+  WarpStage& st = ws[warp];
+  if (lane == 0) {
+    mbar_init(&st.bar, 1);
+    for (int s = 0; s < kMaxSlots; ++s) {
+      st.resident[s] = kNone;
+      st.units[s] = 0;
+    }
+    st.pending_slot = kNone;
+    st.pending_id = kNone;
+    st.pending_units = 0;
+    st.phase = 0;
+    st.victim = 0;
+    st.disabled = 0;
   }
-  for (uint32_t s = tid; s < kMaxSlots; s += blockDim.x) sh.resident[s] = kNone;
-  const uint32_t slot_base = smem_u32(slot_mem);
+  __syncwarp();
   auto lookup = [&](uint32_t loc) -> uint32_t {
     if (loc == kNone) return 0u;
-    const uint32_t d = loc >> kSlotBitsDev;
+    const uint32_t d = loc >> kSlotBitsDev, u = loc & ((1u << kSlotBitsDev) - 1u);
     for (uint32_t s = 0; s < slots; ++s)
-      if (sh.resident[s] == d) return slot_base + s * a.slot_bytes + (loc & ((1u << kSlotBitsDev) - 1u)) * 64u;
+      if (st.resident[s] == d && u < st.units[s]) return slot_base + s * a.slot_bytes + u * 64u;
     return 0u;
   };
-  __syncthreads();
-  for (;;) {
-    // 1. complete the copy started last epoch; clear the vote table
-    if (tid == 0 && sh.pending_slot != kNone) {
-      if (mbar_wait(&sh.bar, sh.phase, kWaitTries)) {
-        sh.resident[sh.pending_slot] = sh.pending_id;
-        sh.phase ^= 1u;
-      } else {
-        sh.disabled = 1;
-        atomicOr(a.status, kStatusTimeout);
-      }
-      sh.pending_slot = kNone;
-      sh.pending_id = kNone;
-    }
-    for (int h = tid; h < kHashSize; h += blockDim.x) {
-      sh.hkey[h] = kNone;
-      sh.hcnt[h] = 0;
-    }
-    __syncthreads();
-    // 2. vote: each active ray's next access -> its treelet
-    const uint32_t nl = w.active() ? w.next_loc() : kNone;
-    const uint32_t key = nl == kNone ? kNone : (nl >> kSlotBitsDev);
-    const uint32_t peers = __match_any_sync(0xffffffffu, key);
-    if (key != kNone && (tid & 31u) == (uint32_t)(__ffs(peers) - 1)) {
-      uint32_t h = (key * 2654435761u) & (kHashSize - 1);
-      for (int probe = 0; probe < kHashSize; ++probe) {
-        const uint32_t old = atomicCAS(&sh.hkey[h], kNone, key);
-        if (old == kNone || old == key) {
-          atomicAdd(&sh.hcnt[h], (uint32_t)__popc(peers));
-          break;
+  Walker<CAP, true> w;
+  bool have = false, exhausted = false;
+  uint32_t r = 0, it = 0;
+  unsigned long long bytes = 0, staged = 0, stagings = 0, sreads = 0, greads = 0;
+  for (;; ++it) {
+    // --- refill idle lanes (as run_persistent)
+    const uint32_t need = __ballot_sync(0xffffffffu, !have);
+    if (!exhausted && need && (__popc(need) >= (int)a.refill || need == 0xffffffffu)) {
+      const int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(a.queue, (uint32_t)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (uint32_t)__popc(need) >= a.n) exhausted = true;
+      if (!have) {
+        const uint32_t rr = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
+        if (rr < a.n) {
+          r = rr;
+          w.init(a, r);
+          have = true;
+          if (!w.active()) {
+            w.finish(a, r);
+            bytes += w.rec.bytes;
+            have = false;
+          }
         }
-        h = (h + 1) & (kHashSize - 1);
       }
     }
-    __syncthreads();
-    // argmax over (count, lowest id), skipping resident treelets
-    unsigned long long bestv = 0;
-    for (int h = tid; h < kHashSize; h += blockDim.x) {
-      const uint32_t k = sh.hkey[h];
-      if (k == kNone) continue;
-      bool res = false;
-      for (uint32_t s = 0; s < slots; ++s) res |= (sh.resident[s] == k);
-      if (res) continue;
-      const unsigned long long v = ((unsigned long long)sh.hcnt[h] << 32) | (unsigned long long)(~k);
-      bestv = v > bestv ? v : bestv;
+    if (!__any_sync(0xffffffffu, have)) {
+      if (exhausted) break;
+      continue;
     }
+    // --- staging: land a finished copy, then vote for the next one
+    if (slots > 0 && (it % a.epoch) == 0) {
+      if (lane == 0 && st.pending_slot != kNone && mbar_test(&st.bar, st.phase)) {
+        st.resident[st.pending_slot] = st.pending_id;
+        st.units[st.pending_slot] = st.pending_units;
+        st.phase ^= 1u;
+        st.pending_slot = kNone;
+      }
+      __syncwarp();
+      if (st.pending_slot == kNone && !st.disabled) {
+        const uint32_t nl = (have && w.active()) ? w.next_loc() : kNone;
+        uint32_t key = nl == kNone ? kNone : (nl >> kSlotBitsDev);
+        if (key != kNone)
+          for (uint32_t s = 0; s < slots; ++s)
+            if (st.resident[s] == key) key = kNone;  // already resident
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        unsigned long long v =
+            key == kNone ? 0ull : (((unsigned long long)__popc(peers) << 32) | (unsigned long long)(~key));
 #pragma unroll
-    for (int s = 16; s > 0; s >>= 1) {
-      const unsigned long long o = __shfl_xor_sync(0xffffffffu, bestv, s);
-      bestv = o > bestv ? o : bestv;
-    }
-    if ((tid & 31u) == 0) sh.best[tid >> 5] = bestv;
-    __syncthreads();
-    if (tid == 0) {
-      unsigned long long b = 0;
-      for (uint32_t k = 0; k < (blockDim.x + 31) / 32; ++k) b = sh.best[k] > b ? sh.best[k] : b;
-      const uint32_t cnt = (uint32_t)(b >> 32);
-      if (cnt > 0 && !sh.disabled && slots > 0) {
-        const uint32_t d = ~(uint32_t)(b & 0xffffffffu);
-        const unsigned long long off = a.image_off[d];
-        const uint32_t bytes = (uint32_t)(a.image_off[d + 1] - off);
-        if (bytes > 0 && bytes <= a.slot_bytes) {
-          const uint32_t s = sh.victim;
-          sh.victim = (s + 1 == slots) ? 0 : s + 1;
-          sh.resident[s] = kNone;
-          mbar_expect_tx(&sh.bar, bytes);
-          bulk_copy_g2s(slot_mem + (size_t)s * a.slot_bytes, reinterpret_cast<const uint8_t*>(a.images) + off, bytes,
-                        &sh.bar);
-          sh.pending_slot = s;
-          sh.pending_id = d;
-          sh.staged_bytes += bytes;
-          sh.stagings += 1;
+        for (int s = 16; s > 0; s >>= 1) {
+          const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, s);
+          v = o > v ? o : v;
+        }
+        const uint32_t votes = (uint32_t)(v >> 32);
+        if (votes > 0 && votes >= a.min_votes && lane == 0) {
+          const uint32_t d = ~(uint32_t)(v & 0xffffffffu);
+          const unsigned long long off = a.image_off[d];
+          uint32_t nb = (uint32_t)(a.image_off[d + 1] - off);
+          if (nb > a.slot_bytes) nb = a.slot_bytes;
+          if (nb > 0) {
+            const uint32_t s = st.victim;
+            st.victim = (s + 1 == slots) ? 0 : s + 1;
+            st.resident[s] = kNone;
+            st.units[s] = 0;
+            mbar_expect_tx(&st.bar, nb);
+            bulk_copy_g2s(my_slots + (size_t)s * a.slot_bytes, reinterpret_cast<const uint8_t*>(a.images) + off, nb,
+                          &st.bar);
+            st.pending_slot = s;
+            st.pending_id = d;
+            st.pending_units = nb / 64u;
+            staged += nb;
+            stagings += 1;
+          }
         }
       }
+      __syncwarp();
     }
-    __syncthreads();
-    // 3. walk
-    for (uint32_t k = 0; k < a.epoch && w.active(); ++k) w.step(a, lookup);
-    if (!__syncthreads_or(w.active() ? 1 : 0)) break;
-  }
-  // a copy still in flight must land before the CTA's shared memory goes away
-  if (tid == 0 && sh.pending_slot != kNone) {
-    if (!mbar_wait(&sh.bar, sh.phase, kWaitTries)) atomicOr(a.status, kStatusTimeout);
-  }
-  if (mine) {
-    w.finish(a, r);
-    if (a.stats) {
-      add_warp_total(a.stats + ST_NODE_BYTES, w.rec.bytes);
-      add_warp_total(a.stats + ST_SMEM_READS, w.smem_reads);
-      add_warp_total(a.stats + ST_GMEM_READS, w.gmem_reads);
+    // --- one node visit per lane
+    if (have) {
+      w.step(a, lookup);
+      if (!w.active()) {
+        w.finish(a, r);
+        bytes += w.rec.bytes;
+        sreads += w.smem_reads;
+        greads += w.gmem_reads;
+        have = false;
+      }
     }
   }
-  if (tid == 0 && a.stats) {
-    atomicAdd(a.stats + ST_STAGED_BYTES, sh.staged_bytes);
-    atomicAdd(a.stats + ST_STAGINGS, sh.stagings);
+  // a copy still in flight must land before the warp's shared memory goes away
+  if (lane == 0 && st.pending_slot != kNone) {
+    if (!mbar_wait(&st.bar, st.phase, kWaitTries)) atomicOr(a.status, kStatusTimeout);
   }
-  __syncthreads();
+  __syncwarp();
+  if (a.stats) {
+    add_warp_total64(a.stats + ST_NODE_BYTES, bytes);
+    add_warp_total64(a.stats + ST_SMEM_READS, sreads);
+    add_warp_total64(a.stats + ST_GMEM_READS, greads);
+    add_warp_total64(a.stats + ST_STAGED_BYTES, staged);
+    add_warp_total64(a.stats + ST_STAGINGS, stagings);
+  }
 }
 
 }  // namespace rtk

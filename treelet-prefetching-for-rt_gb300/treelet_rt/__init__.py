@@ -231,8 +231,10 @@ class Scene:
         check(lib().rt_treelets_remap(self._h, stride, out.ctypes.data))
         return out
 
-    def set_tuning(self, block_threads=0, staged_threads=0, staged_epoch=0, staged_slots=0) -> None:
-        t = Tuning(block_threads, staged_threads, staged_epoch, staged_slots)
+    def set_tuning(self, block_threads=0, staged_threads=0, staged_epoch=0, staged_slots=0, refill_lanes=0,
+                   staged_slot_bytes=0, staged_min_votes=0) -> None:
+        t = Tuning(block_threads, staged_threads, staged_epoch, staged_slots, refill_lanes, staged_slot_bytes,
+                   staged_min_votes)
         check(lib().rt_scene_set_tuning(self._h, C.byref(t)))
 
     def get_tuning(self) -> dict:

@@ -51,7 +51,8 @@ class TreeletInfo(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("staged_threads", C.c_uint32), ("staged_epoch", C.c_uint32),
-                ("staged_slots", C.c_uint32)]
+                ("staged_slots", C.c_uint32), ("refill_lanes", C.c_uint32), ("staged_slot_bytes", C.c_uint32),
+                ("staged_min_votes", C.c_uint32)]
 
 
 class TraceStats(C.Structure):
