@@ -113,6 +113,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+TUNED = os.path.join(REPO, "treelet-prefetching-for-rt_gb300", "treelet_rt", "tuned_gb300.json")
+_tuned_cache = None
+
+
+def apply_tuning(scene, mode_name: str, batch: str) -> dict:
+    """Sets the autotuned launch parameters for (mode, batch kind), if tuned."""
+    global _tuned_cache
+    if _tuned_cache is None:
+        _tuned_cache = {}
+        if os.path.exists(TUNED):
+            with open(TUNED) as f:
+                _tuned_cache = json.load(f).get("results", {})
+    r = _tuned_cache.get(f"{mode_name}/{batch}")
+    if r:
+        scene.set_tuning(**r["tuning"])
+        return r["tuning"]
+    return {}
+
+
 def make_workload(ctx_needed: bool = True):
     import treelet_rt as rt
 
@@ -200,8 +219,12 @@ def run_gpu(args, rank: int, world: int) -> None:
     n_rays = 2 * n_prim
     hit_rate = float(np.frombuffer(d_hits_p.cpu().numpy().tobytes(), rt.HIT_DTYPE)["hit_geometry"].mean())
 
+    names = {rt.MODE_PLAIN: "plain", rt.MODE_TREELET: "treelet", rt.MODE_STAGED: "staged"}
+
     def step(mode):
+        apply_tuning(scene, names[mode], "primary")
         scene.trace(d_prim, d_hits_p, mode, stream=sp, n=n_prim)
+        apply_tuning(scene, names[mode], "bounce")
         scene.trace(d_bounce, d_hits_b, mode, stream=sp, n=n_prim)
 
     def timed(mode, steps, warmup, per_batch=False):
@@ -214,9 +237,11 @@ def run_gpu(args, rank: int, world: int) -> None:
             with torch.cuda.stream(stream):
                 flush.fill_(1.0)
                 e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                apply_tuning(scene, names[mode], "primary")
                 e0.record(stream)
                 scene.trace(d_prim, d_hits_p, mode, stream=sp, n=n_prim)
                 e1.record(stream)
+                apply_tuning(scene, names[mode], "bounce")
                 scene.trace(d_bounce, d_hits_b, mode, stream=sp, n=n_prim)
                 e2.record(stream)
             stream.synchronize()
@@ -283,19 +308,20 @@ def run_gpu(args, rank: int, world: int) -> None:
     h_hits = torch.empty(n_prim * 64, dtype=torch.uint8).pin_memory()
     from treelet_rt._ffi import check, lib
 
-    def host_trace(hr):
+    def host_trace(hr, batch):
+        apply_tuning(scene, "staged", batch)
         check(lib().rt_trace_host(scene.handle, hr.data_ptr(), None, rt.RAY_FLAG_OPAQUE, n_prim, rt.MODE_STAGED,
                                   h_hits.data_ptr(), None))
 
     for _ in range(max(1, args.warmup)):
-        host_trace(h_prim)
+        host_trace(h_prim, "primary")
     e2e_t = []
     for _ in range(max(3, args.steps // 2)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t = time.perf_counter()
-        host_trace(h_prim)
-        host_trace(h_bounce)
+        host_trace(h_prim, "primary")
+        host_trace(h_bounce, "bounce")
         e2e_t.append(time.perf_counter() - t)
     e2e = n_rays / (sum(e2e_t) / len(e2e_t)) / 1e6 * world
 
@@ -322,7 +348,9 @@ def run_gpu(args, rank: int, world: int) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "mode": "staged (treelet order, smem staging)", "l2": "flushed",
                        "treelets": int(tinfo["n_treelets"]), "blob_bytes": int(blob.nbytes()),
-                       "primary_hit_rate": round(hit_rate, 4), "tuning": scene.get_tuning(),
+                       "primary_hit_rate": round(hit_rate, 4),
+                       "tuning": {b: apply_tuning(scene, "staged", b) or scene.get_tuning()
+                                  for b in ("primary", "bounce")},
                        "setup_s": {"scene_gen": round(t_gen, 2), "treelets": round(t_form, 2)}},
             "modes": {k: {kk: round(vv, 3) for kk, vv in v.items()} for k, v in results.items()},
             "staged_hits_equal_treelet_order": staged_exact,
@@ -345,6 +373,179 @@ def run_gpu(args, rank: int, world: int) -> None:
         dist.destroy_process_group()
 
 
+def _time_launch(fn, reps: int, flush, stream) -> float:
+    """Mean milliseconds of fn() over reps (after one warm-up), L2 flushed before each."""
+    import torch
+
+    with torch.cuda.stream(stream):
+        fn()
+    stream.synchronize()
+    ms = []
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        stream.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return sum(ms) / len(ms)
+
+
+def run_ao(args) -> None:
+    """4M triangles in 16 Gaussian blobs (BVH larger than L2); 8 ambient-occlusion
+    rays per primary hit at 1920x1080 (cosine hemisphere, tmax 0.1,
+    TerminateOnFirstHit | Opaque); treelet budget swept over 4/8/16/32 KiB."""
+    import torch
+
+    import treelet_rt as rt
+
+    rt.lib()
+    t0 = time.time()
+    blob = rt.Blob.gen(rt.SCENE_BLOBS, 4 * 1024 * 1024, SEED)
+    prim = rt.camera_rays(rt.default_camera(rt.SCENE_BLOBS), 1920, 1080, 1, SEED, 1e-4, 1e30)
+    ctx = rt.Context(0)
+    scene = rt.Scene(ctx, blob)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    n_p = len(prim)
+    d_prim = torch.from_numpy(prim.view(np.uint8)).cuda()
+    d_hp = torch.empty(n_p * 64, dtype=torch.uint8, device="cuda")
+    scene.trace(d_prim, d_hp, rt.MODE_PLAIN, n=n_p)
+    torch.cuda.synchronize()
+    hits = np.frombuffer(d_hp.cpu().numpy().tobytes(), rt.HIT_DTYPE)
+    hit = np.nonzero(hits["hit_geometry"] == 1)[0]
+    rep_r = np.repeat(prim[hit], 8)
+    rep_h = np.repeat(hits[hit], 8)
+    d_r = torch.from_numpy(rep_r.view(np.uint8).copy()).cuda()
+    d_h = torch.from_numpy(rep_h.view(np.uint8).copy()).cuda()
+    n = len(rep_r)
+    d_ao = torch.empty(n * 32, dtype=torch.uint8, device="cuda")
+    scene.bounce(d_r, d_h, d_ao, seed=SEED + 200, tmin=1e-4, tmax=0.1, n=n)
+    del d_r, d_h
+    d_hits = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    flags = rt.RAY_FLAG_TERMINATE_ON_FIRST_HIT | rt.RAY_FLAG_OPAQUE
+    setup = time.time() - t0
+    table = {}
+    for budget in (4096, 8192, 16384, 32768):
+        info = scene.form_treelets(budget)
+        row = {"treelets": info["n_treelets"]}
+        for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
+            apply_tuning(scene, name, "bounce")
+            ms = _time_launch(lambda: scene.trace(d_ao, d_hits, mode, default_flags=flags, stream=sp, n=n),
+                              max(3, args.steps), flush, stream)
+            row[name] = round(n / ms / 1e3, 3)
+            if name == "staged":
+                st = scene.stats()
+                row["staged_smem_read_fraction"] = round(st["smem_reads"] / max(1, st["smem_reads"] + st["gmem_reads"]), 4)
+                row["node_bytes"] = st["node_bytes"]
+        table[str(budget)] = row
+    line = {"metric": "Mrays/s, AO any-hit rays, treelet budget sweep", "unit": "Mrays/s",
+            "value": max(r["staged"] for r in table.values()), "higher_is_better": True, "n_gpus": 1,
+            "config": {"workload": "4M triangles in 16 Gaussian blobs (sigma 0.05), 1920x1080 primary, 8 AO rays per "
+                                   "hit (tmax 0.1, TerminateOnFirstHit|Opaque)",
+                       "ao_rays": n, "primary_hit_rate": round(len(hit) / n_p, 4), "blob_bytes": blob.nbytes(),
+                       "l2": "flushed", "setup_s": round(setup, 1)},
+            "budgets": table, "dtype": "f32", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args) -> None:
+    """256 scenes of log-uniform size (1K..1M triangles, unit-cube generator),
+    each with a log-uniform ray batch (4K..256K rays, half primary, half
+    bounce): one persistent work-queue launch (and its CUDA-graph replay)
+    against one launch per scene."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+
+    import treelet_rt as rt
+
+    rt.lib()
+    rng = np.random.default_rng(SEED)
+    n_scenes = args.scenes
+    tris = np.exp(rng.uniform(np.log(1e3), np.log(1e6), n_scenes)).astype(np.int64)
+    nrays = np.exp(rng.uniform(np.log(4096), np.log(262144), n_scenes)).astype(np.int64)
+    t0 = time.time()
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        blobs = list(ex.map(lambda i: rt.Blob.gen(rt.SCENE_CUBE, int(tris[i]), SEED + i), range(n_scenes)))
+    t_build = time.time() - t0
+    ctx = rt.Context(0)
+    scenes = []
+    for b in blobs:
+        s = rt.Scene(ctx, b)
+        s.form_treelets(BUDGET)
+        scenes.append(s)
+    cam = rt.default_camera(rt.SCENE_CUBE)
+    rays, begin, item_scene = [], [0], []
+    for i, s in enumerate(scenes):
+        half = int(nrays[i]) // 2
+        w = max(8, int(np.sqrt(half)))
+        h = max(4, half // w)
+        p = rt.camera_rays(cam, w, h, 1, SEED + i, 1e-4, 1e30)
+        d_p = torch.from_numpy(p.view(np.uint8).copy()).cuda()
+        d_h = torch.empty(len(p) * 64, dtype=torch.uint8, device="cuda")
+        d_b = torch.empty(len(p) * 32, dtype=torch.uint8, device="cuda")
+        s.trace(d_p, d_h, rt.MODE_PLAIN, n=len(p))
+        s.bounce(d_p, d_h, d_b, seed=SEED + 1000 + i, n=len(p))
+        torch.cuda.synchronize()
+        b = np.frombuffer(d_b.cpu().numpy().tobytes(), rt.RAY_DTYPE)
+        r = np.concatenate([p, b])
+        rays.append(r)
+        begin.append(begin[-1] + len(r))
+        item_scene.append(i)
+    rays = np.concatenate(rays)
+    n = len(rays)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+    d_hits2 = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+    batch = rt.Batch(ctx, scenes)
+    batch.set_items(begin, item_scene)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    ray_bytes = d_rays.data_ptr()
+    hit_bytes = d_hits2.data_ptr()
+    out = {}
+    for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET)):
+        for s in scenes:
+            apply_tuning(s, name, "bounce")
+        tuned = apply_tuning(scenes[0], name, "bounce")
+        if tuned:
+            batch.set_tuning(**tuned)
+
+        def per_scene():
+            for i, s in enumerate(scenes):
+                b0, b1 = begin[i], begin[i + 1]
+                rt.lib().rt_trace(s.handle, C_void(ray_bytes + 32 * b0), None, rt.RAY_FLAG_OPAQUE, b1 - b0, mode,
+                                  C_void(hit_bytes + 64 * b0), None, C_void(sp))
+
+        ms_scene = _time_launch(per_scene, max(3, args.steps), flush, stream)
+        ms_batch = _time_launch(lambda: batch.trace(d_rays, d_hits, mode, stream=sp), max(3, args.steps), flush,
+                                stream)
+        batch.capture(d_rays, d_hits, mode, stream=sp)
+        ms_graph = _time_launch(lambda: batch.replay(stream=sp), max(3, args.steps), flush, stream)
+        same = bool(torch.equal(d_hits, d_hits2))
+        out[name] = {"per_scene_launches_mrays_s": round(n / ms_scene / 1e3, 3),
+                     "one_launch_mrays_s": round(n / ms_batch / 1e3, 3),
+                     "graph_replay_mrays_s": round(n / ms_graph / 1e3, 3), "hits_equal": same}
+    line = {"metric": "Mrays/s, 256 scenes in one persistent work-queue launch vs one launch per scene",
+            "unit": "Mrays/s", "value": out["plain"]["graph_replay_mrays_s"], "higher_is_better": True, "n_gpus": 1,
+            "config": {"workload": f"{n_scenes} scenes, triangles log-uniform 1K..1M (total {int(tris.sum())}), rays "
+                                   f"log-uniform 4K..256K per scene (total {n}), half primary half bounce",
+                       "build_s": round(t_build, 1), "l2": "flushed"},
+            "modes": out, "dtype": "f32", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
+def C_void(v: int):
+    import ctypes
+
+    return ctypes.c_void_p(v)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -355,7 +556,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="small: the same scene with 512x512x1 primary rays + bounces (profiling case)")
+    ap.add_argument("--workload", default="terrain", choices=["terrain", "ao", "batch"],
+                    help="terrain: the headline line; ao: AO budget sweep; batch: many scenes in one launch")
+    ap.add_argument("--scenes", type=int, default=256)
     args = ap.parse_args()
+    if args.workload == "ao" and args.impl != "reference":
+        return run_ao(args)
+    if args.workload == "batch" and args.impl != "reference":
+        return run_batch(args)
     if args.size == "small":
         global WIDTH, HEIGHT, SPP, WORKLOAD
         WIDTH = HEIGHT = 512

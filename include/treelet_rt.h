@@ -265,6 +265,7 @@ typedef struct rt_tuning {
   uint32_t refill_lanes;      /* idle lanes of a warp that make it fetch new rays (1..32) */
   uint32_t staged_slot_bytes; /* bytes per slot: a treelet's first bytes when smaller than it */
   uint32_t staged_min_votes;  /* lanes of a warp that must want a treelet to stage it (1..32) */
+  uint32_t stack_depth;       /* traversal stack entries per ray: 48, 96 or 160 (deeper rays are flagged) */
 } rt_tuning;
 rt_status rt_scene_set_tuning(rt_scene* scene, const rt_tuning* t);
 rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);
@@ -285,6 +286,27 @@ rt_status rt_trace_stats_get(rt_scene* scene, rt_trace_stats* out);
 /* Device version of rt_gen_bounce_rays_host (stream-ordered). */
 rt_status rt_gen_bounce_rays(rt_scene* scene, const rt_ray* rays, const rt_hit* hits, uint32_t n, uint64_t seed,
                              float tmin, float tmax, rt_ray* out, void* stream);
+
+/* ---------------- many scenes, one launch ---------------- */
+
+/* A batch traces rays of many scenes in ONE persistent work-queue launch
+ * (no reference counterpart: the reference traces one ray per call).  Item k
+ * covers rays [ray_begin[k], ray_begin[k+1]) of the concatenated ray and hit
+ * arrays and uses scenes[item_scene[k]].  Modes PLAIN and TREELET (every
+ * scene needs rt_treelets_form for TREELET).  The batch owns its queue and
+ * counter memory; the scenes must outlive it. */
+typedef struct rt_batch rt_batch;
+rt_status rt_batch_create(rt_ctx* ctx, rt_scene* const* scenes, uint32_t n_scenes, rt_batch** out);
+rt_status rt_batch_destroy(rt_batch* b);
+rt_status rt_batch_set_items(rt_batch* b, const uint32_t* ray_begin, const uint32_t* item_scene, uint32_t n_items);
+rt_status rt_batch_set_tuning(rt_batch* b, const rt_tuning* t);
+rt_status rt_trace_batch(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
+                         uint32_t mode, rt_hit* hits, void* stream);
+/* Records rt_trace_batch with these buffers into a CUDA graph owned by the
+ * batch (replacing any previous one); rt_batch_graph_launch replays it. */
+rt_status rt_batch_graph_capture(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
+                                 uint32_t mode, rt_hit* hits, void* stream);
+rt_status rt_batch_graph_launch(rt_batch* b, void* stream);
 
 /* ---------------- treelet-prefetch decision ---------------- */
 

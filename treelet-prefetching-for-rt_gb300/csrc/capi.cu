@@ -115,7 +115,7 @@ struct rt_scene {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
-  rt_tuning tuning{128, 128, 4, 1, 8, 0, 2};
+  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96};
   // host-buffer path scratch
   cudaStream_t stream = nullptr;
   void* d_io = nullptr;
@@ -179,6 +179,58 @@ int max_smem_per_block() {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   return v;
+}
+
+// Zeroes the launch's counters and queue, then launches the kernel of `mode`
+// with stack depth CAP.
+template <int CAP>
+rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint32_t largest_image, cudaStream_t st) {
+  a.epoch = t.staged_epoch;
+  a.refill = t.refill_lanes;
+  RT_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, st));
+  RT_CUDA(cudaMemsetAsync(a.status, 0, sizeof(uint32_t), st));
+  RT_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), st));
+  if (mode == RT_MODE_PLAIN) {
+    const uint32_t bt = t.block_threads;
+    auto kern = rtk::trace_plain_kernel<CAP>;
+    kern<<<persistent_grid((const void*)kern, bt, a.n), bt, 0, st>>>(a);
+  } else if (mode == RT_MODE_TREELET) {
+    const uint32_t bt = t.block_threads;
+    auto kern = rtk::trace_treelet_kernel<CAP>;
+    kern<<<persistent_grid((const void*)kern, bt, a.n), bt, 0, st>>>(a);
+  } else {
+    const uint32_t bt = t.staged_threads;
+    const uint32_t warps = bt / 32;
+    // per-warp slots: the whole largest image, or the first staged_slot_bytes of each
+    uint32_t slot_bytes = largest_image;
+    if (t.staged_slot_bytes) slot_bytes = std::min(slot_bytes, (t.staged_slot_bytes + 127u) & ~127u);
+    uint32_t slots = t.staged_slots;
+    const int limit = max_smem_per_block() - (int)(sizeof(rtk::WarpStage) * 8) - 1024;
+    while (slots > 0 && (int)(warps * slots * slot_bytes + 128) > limit) --slots;
+    a.slots = slots;
+    a.slot_bytes = slot_bytes;
+    a.min_votes = t.staged_min_votes;
+    const size_t dyn = (size_t)warps * slots * slot_bytes + 128;
+    auto kern = rtk::trace_staged_kernel<CAP>;
+    RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    kern<<<persistent_grid((const void*)kern, bt, a.n, dyn), bt, dyn, st>>>(a);
+  }
+  RT_CUDA(cudaGetLastError());
+  return RT_OK;
+}
+
+// Stack depths compiled in (entries per stack per ray); a ray that needs more
+// is flagged RT_RAY_STACK_OVERFLOW.
+rt_status launch_trace(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint32_t largest_image,
+                       cudaStream_t st) {
+  switch (t.stack_depth) {
+    case 48:
+      return launch_cap<48>(a, mode, t, largest_image, st);
+    case 160:
+      return launch_cap<160>(a, mode, t, largest_image, st);
+    default:
+      return launch_cap<96>(a, mode, t, largest_image, st);
+  }
 }
 
 }  // namespace
@@ -366,6 +418,11 @@ rt_status rt_scene_set_tuning(rt_scene* s, const rt_tuning* t) {
     if (t->staged_min_votes > 32) return rti::fail(RT_ERR_INVALID, "staged_min_votes must be 1..32");
     n.staged_min_votes = t->staged_min_votes;
   }
+  if (t->stack_depth) {
+    if (t->stack_depth != 48 && t->stack_depth != 96 && t->stack_depth != 160)
+      return rti::fail(RT_ERR_INVALID, "stack_depth must be 48, 96 or 160");
+    n.stack_depth = t->stack_depth;
+  }
   s->tuning = n;
   return RT_OK;
 }
@@ -387,6 +444,8 @@ rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint3
     return rti::fail(RT_ERR_STATE, "rt_trace: call rt_treelets_form first");
   if (trace && (trace->visits || trace->treelets) && trace->capacity == 0)
     return rti::fail(RT_ERR_INVALID, "rt_trace: trace capacity is 0");
+  if (mode == RT_MODE_STAGED && s->part.roots.size() >= rtt::kMaxDense)
+    return rti::fail(RT_ERR_TOO_LARGE, "rt_trace: too many treelets for staged mode (max 4194304)");
   cudaStream_t st = (cudaStream_t)stream;
   RT_CUDA(cudaSetDevice(s->ctx->device));
   rtk::TraceArgs a{};
@@ -406,41 +465,8 @@ rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint3
   a.n_treelets = s->has_treelets ? (uint32_t)s->part.roots.size() : 0;
   a.stats = s->d_stats;
   a.status = s->d_status;
-  a.epoch = s->tuning.staged_epoch;
   a.queue = s->d_queue;
-  a.refill = s->tuning.refill_lanes;
-  RT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, st));
-  RT_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), st));
-  RT_CUDA(cudaMemsetAsync(s->d_queue, 0, sizeof(uint32_t), st));
-  if (mode == RT_MODE_PLAIN) {
-    const uint32_t bt = s->tuning.block_threads;
-    auto kern = rtk::trace_plain_kernel<kPlainCap>;
-    kern<<<persistent_grid((const void*)kern, bt, n), bt, 0, st>>>(a);
-  } else if (mode == RT_MODE_TREELET) {
-    const uint32_t bt = s->tuning.block_threads;
-    auto kern = rtk::trace_treelet_kernel<kTreeletCap>;
-    kern<<<persistent_grid((const void*)kern, bt, n), bt, 0, st>>>(a);
-  } else {
-    if (s->part.roots.size() >= rtt::kMaxDense)
-      return rti::fail(RT_ERR_TOO_LARGE, "rt_trace: too many treelets for staged mode (max 4194304)");
-    const uint32_t bt = s->tuning.staged_threads;
-    const uint32_t warps = bt / 32;
-    // per-warp slots: the whole largest image, or the first staged_slot_bytes of each
-    uint32_t slot_bytes = s->slot_bytes;
-    if (s->tuning.staged_slot_bytes) slot_bytes = std::min(slot_bytes, (s->tuning.staged_slot_bytes + 127u) & ~127u);
-    uint32_t slots = s->tuning.staged_slots;
-    const int limit = max_smem_per_block() - (int)(sizeof(rtk::WarpStage) * 8) - 1024;
-    while (slots > 0 && (int)(warps * slots * slot_bytes + 128) > limit) --slots;
-    a.slots = slots;
-    a.slot_bytes = slot_bytes;
-    a.min_votes = s->tuning.staged_min_votes;
-    const size_t dyn = (size_t)warps * slots * slot_bytes + 128;
-    auto kern = rtk::trace_staged_kernel<kTreeletCap>;
-    RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-    kern<<<persistent_grid((const void*)kern, bt, n, dyn), bt, dyn, st>>>(a);
-  }
-  RT_CUDA(cudaGetLastError());
-  return RT_OK;
+  return launch_trace(a, mode, s->tuning, s->slot_bytes, st);
 }
 
 rt_status rt_trace_stats_get(rt_scene* s, rt_trace_stats* out) {
@@ -568,3 +594,181 @@ extern "C" rt_status rt_prefetch_decide(rt_scene* s, const uint32_t* next_unit, 
   RT_CUDA(cudaGetLastError());
   return RT_OK;
 }
+
+// ------------------------------------------------------------ batches
+struct rt_batch {
+  rt_ctx* ctx = nullptr;
+  std::vector<rt_scene*> scenes;
+  rtk::SceneView* d_views = nullptr;
+  uint32_t* d_item_begin = nullptr;
+  uint32_t* d_item_scene = nullptr;
+  uint32_t n_items = 0, n_rays = 0;
+  unsigned long long* d_stats = nullptr;
+  uint32_t* d_status = nullptr;
+  uint32_t* d_queue = nullptr;
+  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+void free_graph(rt_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+rt_status batch_args(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t mode,
+                     rt_hit* hits, rtk::TraceArgs& a) {
+  if (!rays || !hits) return rti::fail(RT_ERR_INVALID, "rt_trace_batch: NULL rays or hits");
+  if (mode != RT_MODE_PLAIN && mode != RT_MODE_TREELET)
+    return rti::fail(RT_ERR_INVALID, "rt_trace_batch: batches run RT_MODE_PLAIN or RT_MODE_TREELET");
+  if (b->n_items == 0) return rti::fail(RT_ERR_STATE, "rt_trace_batch: call rt_batch_set_items first");
+  if (mode == RT_MODE_TREELET)
+    for (rt_scene* s : b->scenes)
+      if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_trace_batch: a scene has no treelets");
+  a = rtk::TraceArgs{};
+  a.scenes = b->d_views;
+  a.item_begin = b->d_item_begin;
+  a.item_scene = b->d_item_scene;
+  a.n_items = b->n_items;
+  a.rays = rays;
+  a.flags = flags;
+  a.default_flags = default_flags;
+  a.n = b->n_rays;
+  a.hits = hits;
+  a.stats = b->d_stats;
+  a.status = b->d_status;
+  a.queue = b->d_queue;
+  return RT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rt_status rt_batch_create(rt_ctx* ctx, rt_scene* const* scenes, uint32_t n_scenes, rt_batch** out) {
+  if (!ctx || !scenes || !out || n_scenes == 0) return rti::fail(RT_ERR_INVALID, "rt_batch_create: bad argument");
+  *out = nullptr;
+  RT_CUDA(cudaSetDevice(ctx->device));
+  auto* b = new rt_batch();
+  b->ctx = ctx;
+  b->scenes.assign(scenes, scenes + n_scenes);
+  rt_status st = dalloc(&b->d_views, sizeof(rtk::SceneView) * n_scenes);
+  if (st == RT_OK) st = dalloc(&b->d_stats, sizeof(unsigned long long) * rtk::ST_COUNT);
+  if (st == RT_OK) st = dalloc(&b->d_status, sizeof(uint32_t));
+  if (st == RT_OK) st = dalloc(&b->d_queue, sizeof(uint32_t));
+  if (st != RT_OK) {
+    rt_batch_destroy(b);
+    return st;
+  }
+  std::vector<rtk::SceneView> v(n_scenes);
+  for (uint32_t i = 0; i < n_scenes; ++i) {
+    if (!scenes[i] || scenes[i]->ctx->device != ctx->device) {
+      rt_batch_destroy(b);
+      return rti::fail(RT_ERR_INVALID, "rt_batch_create: NULL scene or scene on another device");
+    }
+    v[i] = rtk::SceneView{reinterpret_cast<const uint4*>(scenes[i]->d_blob), scenes[i]->d_meta, scenes[i]->n_units};
+  }
+  cudaError_t e = cudaMemcpy(b->d_views, v.data(), sizeof(rtk::SceneView) * n_scenes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    rt_batch_destroy(b);
+    return cuda_fail(e, "rt_batch_create");
+  }
+  *out = b;
+  return RT_OK;
+}
+
+rt_status rt_batch_destroy(rt_batch* b) {
+  if (!b) return RT_OK;
+  free_graph(b);
+  cudaFree(b->d_views);
+  cudaFree(b->d_item_begin);
+  cudaFree(b->d_item_scene);
+  cudaFree(b->d_stats);
+  cudaFree(b->d_status);
+  cudaFree(b->d_queue);
+  delete b;
+  return RT_OK;
+}
+
+rt_status rt_batch_set_items(rt_batch* b, const uint32_t* ray_begin, const uint32_t* item_scene, uint32_t n_items) {
+  if (!b || !ray_begin || !item_scene || n_items == 0) return rti::fail(RT_ERR_INVALID, "rt_batch_set_items: bad argument");
+  for (uint32_t k = 0; k < n_items; ++k) {
+    if (ray_begin[k + 1] < ray_begin[k]) return rti::fail(RT_ERR_INVALID, "rt_batch_set_items: ray_begin not ascending");
+    if (item_scene[k] >= b->scenes.size()) return rti::fail(RT_ERR_INVALID, "rt_batch_set_items: scene index");
+  }
+  if (ray_begin[0] != 0) return rti::fail(RT_ERR_INVALID, "rt_batch_set_items: ray_begin[0] must be 0");
+  RT_CUDA(cudaSetDevice(b->ctx->device));
+  free_graph(b);
+  cudaFree(b->d_item_begin);
+  cudaFree(b->d_item_scene);
+  b->d_item_begin = nullptr;
+  b->d_item_scene = nullptr;
+  rt_status st = dalloc(&b->d_item_begin, sizeof(uint32_t) * (n_items + 1));
+  if (st == RT_OK) st = dalloc(&b->d_item_scene, sizeof(uint32_t) * n_items);
+  if (st != RT_OK) return st;
+  RT_CUDA(cudaMemcpy(b->d_item_begin, ray_begin, sizeof(uint32_t) * (n_items + 1), cudaMemcpyHostToDevice));
+  RT_CUDA(cudaMemcpy(b->d_item_scene, item_scene, sizeof(uint32_t) * n_items, cudaMemcpyHostToDevice));
+  b->n_items = n_items;
+  b->n_rays = ray_begin[n_items];
+  return RT_OK;
+}
+
+rt_status rt_batch_set_tuning(rt_batch* b, const rt_tuning* t) {
+  if (!b || !t || b->scenes.empty()) return rti::fail(RT_ERR_INVALID, "rt_batch_set_tuning: NULL");
+  // validate through a scene's setter, then keep a copy for the batch
+  rt_tuning keep = b->scenes[0]->tuning;
+  rt_status st = rt_scene_set_tuning(b->scenes[0], t);
+  if (st != RT_OK) return st;
+  b->tuning = b->scenes[0]->tuning;
+  b->scenes[0]->tuning = keep;
+  return RT_OK;
+}
+
+rt_status rt_trace_batch(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t mode,
+                         rt_hit* hits, void* stream) {
+  if (!b) return rti::fail(RT_ERR_INVALID, "rt_trace_batch: NULL batch");
+  rtk::TraceArgs a;
+  rt_status st = batch_args(b, rays, flags, default_flags, mode, hits, a);
+  if (st != RT_OK) return st;
+  if (b->n_rays == 0) return RT_OK;
+  RT_CUDA(cudaSetDevice(b->ctx->device));
+  return launch_trace(a, mode, b->tuning, 0, (cudaStream_t)stream);
+}
+
+rt_status rt_batch_graph_capture(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
+                                 uint32_t mode, rt_hit* hits, void* stream) {
+  if (!b) return rti::fail(RT_ERR_INVALID, "rt_batch_graph_capture: NULL batch");
+  if (!stream) return rti::fail(RT_ERR_INVALID, "rt_batch_graph_capture: capture needs a non-default stream");
+  rtk::TraceArgs a;
+  rt_status st = batch_args(b, rays, flags, default_flags, mode, hits, a);
+  if (st != RT_OK) return st;
+  RT_CUDA(cudaSetDevice(b->ctx->device));
+  free_graph(b);
+  cudaStream_t s = (cudaStream_t)stream;
+  // the kernel attributes and launch shapes are resolved outside the capture
+  RT_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  st = launch_trace(a, mode, b->tuning, 0, s);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (st != RT_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "rt_batch_graph_capture: cudaStreamEndCapture");
+  b->graph = g;
+  RT_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  return RT_OK;
+}
+
+rt_status rt_batch_graph_launch(rt_batch* b, void* stream) {
+  if (!b || !b->exec) return rti::fail(RT_ERR_STATE, "rt_batch_graph_launch: no captured graph");
+  RT_CUDA(cudaSetDevice(b->ctx->device));
+  RT_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+  return RT_OK;
+}
+
+}  // extern "C"

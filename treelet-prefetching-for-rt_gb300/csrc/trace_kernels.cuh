@@ -33,9 +33,22 @@ enum Stat { ST_NODE_BYTES = 0, ST_STAGED_BYTES, ST_SMEM_READS, ST_GMEM_READS, ST
 // Status word bits set by kernels (device-wide, not per ray).
 constexpr uint32_t kStatusTimeout = 1u;
 
+// What a walk needs of one scene.
+struct SceneView {
+  const uint4* blob;
+  const uint2* meta;  // per unit: x = treelet root unit, y = dense << 10 | slot
+  uint32_t n_units;
+};
+
 struct TraceArgs {
   const uint4* blob;
   uint32_t n_units;
+  // several scenes in one launch: rays [item_begin[k], item_begin[k+1]) use
+  // scenes[item_scene[k]]; n_items == 0 means every ray uses blob / meta
+  const SceneView* scenes;
+  const uint32_t* item_begin;
+  const uint32_t* item_scene;
+  uint32_t n_items;
   const rt_ray* rays;
   const uint32_t* flags;
   uint32_t default_flags;
@@ -85,8 +98,25 @@ __device__ __forceinline__ void load_ray(const rt_ray* rays, uint32_t r, rtm::V3
   tmax = b.w;
 }
 
+// The scene ray r walks.
+__device__ __forceinline__ SceneView scene_of(const TraceArgs& a, uint32_t r) {
+  if (a.n_items == 0) return SceneView{a.blob, a.meta, a.n_units};
+  uint32_t lo = 0, hi = a.n_items;  // last item with item_begin <= r
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(a.item_begin + mid) <= r) lo = mid;
+    else hi = mid;
+  }
+  const SceneView* s = a.scenes + __ldg(a.item_scene + lo);
+  SceneView v;
+  v.blob = reinterpret_cast<const uint4*>(__ldg(reinterpret_cast<const unsigned long long*>(&s->blob)));
+  v.meta = reinterpret_cast<const uint2*>(__ldg(reinterpret_cast<const unsigned long long*>(&s->meta)));
+  v.n_units = __ldg(&s->n_units);
+  return v;
+}
+
 // Hit record from the closest leaf / instance (vulkan_ray_tracing.cc:2990-3028).
-__device__ __forceinline__ void write_hit(const TraceArgs& a, uint32_t r, bool hit, float min_thit, rtm::V3 O,
+__device__ __forceinline__ void write_hit(const TraceArgs& a, const SceneView& v, uint32_t r, bool hit, float min_thit, rtm::V3 O,
                                           rtm::V3 D, float tmin, float tmax, uint32_t c_leaf, uint32_t c_inst,
                                           float c_tobj, const Recorder& rec, uint32_t status) {
   rt_hit h;
@@ -102,9 +132,9 @@ __device__ __forceinline__ void write_hit(const TraceArgs& a, uint32_t r, bool h
   h.reserved = 0;
   if (hit) {
     rtd::Node64 q;
-    rtd::load64(a.blob + (uint64_t)c_leaf * 4, 0, q);
+    rtd::load64(v.blob + (uint64_t)c_leaf * 4, 0, q);
     rtd::Instance in;
-    rtd::load_instance(a.blob + (uint64_t)c_inst * 4, 0, in);
+    rtd::load_instance(v.blob + (uint64_t)c_inst * 4, 0, in);
     const rtm::ObjRay orr = rtm::make_transformed_ray(in.w2o, O, D, tmin, tmax);
     h.hit_geometry = 1;
     h.geometry_index = rtf::geometry_index_of(q.w[1]);
@@ -230,6 +260,7 @@ struct PlainWalker {
   InstCtx ic;
   bool ic_fast;
   Recorder rec;
+  SceneView v;
 
   __device__ __forceinline__ bool active() const { return next != kNone || sp > 0; }
 
@@ -239,12 +270,13 @@ struct PlainWalker {
   }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
+    v = scene_of(a, r);
     load_ray(a.rays, r, O, tmin, D, tmax);
     const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
     terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
     opaque = flags & rtf::RAY_FLAG_OPAQUE;
     rec = Recorder{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
-                   a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, a.meta};
+                   a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, v.meta};
     status = 0;
     sp = 0;
     next = kNone;
@@ -257,7 +289,7 @@ struct PlainWalker {
     idir = rtm::calculate_idir(D);
     fast = rtd::finite_ray(O, D, tmin, tmax);
     rec.rec(0, rtf::TX_STRUCTURE);
-    const uint4 h0 = __ldg(a.blob), h1 = __ldg(a.blob + 1);
+    const uint4 h0 = __ldg(v.blob), h1 = __ldg(v.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
     const rtm::V3 bmax = rtm::v3(__uint_as_float(h1.y), __uint_as_float(h1.z), __uint_as_float(h1.w));
@@ -272,10 +304,10 @@ struct PlainWalker {
   }
 
   __device__ __forceinline__ void visit_internal(const TraceArgs& a, uint32_t unit) {
-    if (unit >= a.n_units) return stop(RT_RAY_BAD_NODE);
+    if (unit >= v.n_units) return stop(RT_RAY_BAD_NODE);
     rec.rec(unit, rtf::TX_INTERNAL);
     rtd::Node64 nd;
-    rtd::load64(a.blob + (uint64_t)unit * 4, 0, nd);
+    rtd::load64(v.blob + (uint64_t)unit * 4, 0, nd);
     rtd::ChildHits ch;
     if (inblas) {
       const float cull = min_thit * ic.mult;
@@ -302,10 +334,10 @@ struct PlainWalker {
   }
 
   __device__ __forceinline__ void visit_leaf(const TraceArgs& a, uint32_t unit) {
-    if (unit >= a.n_units) return stop(RT_RAY_BAD_NODE);
+    if (unit >= v.n_units) return stop(RT_RAY_BAD_NODE);
     rec.rec(unit, rtf::TX_LEAF_DESC);
     rtd::Node64 q;
-    rtd::load64(a.blob + (uint64_t)unit * 4, 0, q);
+    rtd::load64(v.blob + (uint64_t)unit * 4, 0, q);
     if (rtf::leaf_type_of(q.w[1]) == 0) {
       const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
       const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
@@ -330,14 +362,14 @@ struct PlainWalker {
   }
 
   __device__ __forceinline__ void visit_instance(const TraceArgs& a, uint32_t unit) {
-    if (unit + 1 >= a.n_units) return stop(RT_RAY_BAD_NODE);
+    if (unit + 1 >= v.n_units) return stop(RT_RAY_BAD_NODE);
     rec.rec(unit, rtf::TX_INSTANCE_LEAF);
     rtd::Instance in;
-    rtd::load_instance(a.blob + (uint64_t)unit * 4, 0, in);
+    rtd::load_instance(v.blob + (uint64_t)unit * 4, 0, in);
     const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
-    if ((hdr & 63) || hdr / 64 >= a.n_units) return stop(RT_RAY_BAD_NODE);
+    if ((hdr & 63) || hdr / 64 >= v.n_units) return stop(RT_RAY_BAD_NODE);
     rec.rec((uint32_t)(hdr >> 6), rtf::TX_STRUCTURE);
-    const uint4 h0 = __ldg(a.blob + (hdr >> 4));
+    const uint4 h0 = __ldg(v.blob + (hdr >> 4));
     const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
     enter_instance(in, unit, O, D, tmin, tmax, ic);
     ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
@@ -372,7 +404,7 @@ struct PlainWalker {
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
     const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);
-    write_hit(a, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
+    write_hit(a, v, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
   }
 };
 

@@ -24,6 +24,7 @@ struct Walker {
   uint32_t cu_loc[STAGED ? CAP : 1], ot_loc[STAGED ? CAP : 1];
   InstCtx ic;
   Recorder rec;
+  SceneView v;
   uint32_t smem_reads, gmem_reads;
 
   __device__ __forceinline__ bool active() const { return cn > 0 || on > 0; }
@@ -40,13 +41,13 @@ struct Walker {
   __device__ __forceinline__ void route(const TraceArgs& a, uint32_t code, uint32_t inst) {
     const uint32_t unit = code >> 2;
     uint32_t root = kNone, loc = kNone;
-    if (unit < a.n_units) {
+    if (unit < v.n_units) {
       if (STAGED) {
-        const uint2 m = __ldg(a.meta + unit);
+        const uint2 m = __ldg(v.meta + unit);
         root = m.x;
         loc = m.y;
       } else {
-        root = __ldg(reinterpret_cast<const uint32_t*>(a.meta) + 2ull * unit);
+        root = __ldg(reinterpret_cast<const uint32_t*>(v.meta) + 2ull * unit);
       }
     }
     const unsigned long long e = (unsigned long long)code | ((unsigned long long)inst << 32);
@@ -70,11 +71,12 @@ struct Walker {
   }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
+    v = scene_of(a, r);
     load_ray(a.rays, r, O, tmin, D, tmax);
     const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
     terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
     rec = Recorder{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
-                   a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, a.meta};
+                   a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, v.meta};
     status = 0;
     cn = on = 0;
     min_thit = tmax;
@@ -87,7 +89,7 @@ struct Walker {
     fast = rtd::finite_ray(O, D, tmin, tmax);
     ic_fast = false;
     rec.rec(0, rtf::TX_STRUCTURE);
-    const uint4 h0 = __ldg(a.blob), h1 = __ldg(a.blob + 1);
+    const uint4 h0 = __ldg(v.blob), h1 = __ldg(v.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
     const rtm::V3 bmax = rtm::v3(__uint_as_float(h1.y), __uint_as_float(h1.z), __uint_as_float(h1.w));
@@ -98,7 +100,7 @@ struct Walker {
   __device__ __forceinline__ void ensure_instance(const TraceArgs& a, uint32_t inst) {
     if (ic.unit == inst) return;
     rtd::Instance in;
-    rtd::load_instance(a.blob + (uint64_t)inst * 4, 0, in);
+    rtd::load_instance(v.blob + (uint64_t)inst * 4, 0, in);
     enter_instance(in, inst, O, D, tmin, tmax, ic);
     ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
   }
@@ -122,7 +124,7 @@ struct Walker {
     const uint32_t code = (uint32_t)e, inst = (uint32_t)(e >> 32);
     const uint32_t unit = code >> 2;
     const bool top = code & kTop, leaf = code & kLeaf;
-    if (unit + ((top && leaf) ? 1u : 0u) >= a.n_units) {
+    if (unit + ((top && leaf) ? 1u : 0u) >= v.n_units) {
       status |= RT_RAY_BAD_NODE;
       cn = on = 0;
       return;
@@ -133,7 +135,7 @@ struct Walker {
       if (saddr) ++smem_reads;
       else ++gmem_reads;
     }
-    const uint4* g = a.blob + (uint64_t)unit * 4;
+    const uint4* g = v.blob + (uint64_t)unit * 4;
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
       rec.rec(unit, rtf::TX_INTERNAL);
       rtd::Node64 nd;
@@ -164,13 +166,13 @@ struct Walker {
       rtd::Instance in;
       rtd::load_instance(g, saddr, in);
       const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
-      if ((hdr & 63) || hdr / 64 >= a.n_units) {
+      if ((hdr & 63) || hdr / 64 >= v.n_units) {
         status |= RT_RAY_BAD_NODE;
         cn = on = 0;
         return;
       }
       rec.rec((uint32_t)(hdr >> 6), rtf::TX_STRUCTURE);
-      const uint4 h0 = __ldg(a.blob + (hdr >> 4));
+      const uint4 h0 = __ldg(v.blob + (hdr >> 4));
       const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
       enter_instance(in, unit, O, D, tmin, tmax, ic);
       ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
@@ -211,7 +213,7 @@ struct Walker {
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
     const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);
-    write_hit(a, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
+    write_hit(a, v, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
   }
 };
 

@@ -232,9 +232,9 @@ class Scene:
         return out
 
     def set_tuning(self, block_threads=0, staged_threads=0, staged_epoch=0, staged_slots=0, refill_lanes=0,
-                   staged_slot_bytes=0, staged_min_votes=0) -> None:
+                   staged_slot_bytes=0, staged_min_votes=0, stack_depth=0) -> None:
         t = Tuning(block_threads, staged_threads, staged_epoch, staged_slots, refill_lanes, staged_slot_bytes,
-                   staged_min_votes)
+                   staged_min_votes, stack_depth)
         check(lib().rt_scene_set_tuning(self._h, C.byref(t)))
 
     def get_tuning(self) -> dict:
@@ -282,3 +282,47 @@ class Scene:
                         stream: int = 0) -> None:
         check(lib().rt_prefetch_decide(self._h, ptr(next_unit), n_units, lanes, C.byref(params), ptr(state), ptr(out),
                                        C.c_void_p(stream)))
+
+
+class Batch:
+    """Several scenes traced in one persistent work-queue launch (optionally
+    replayed from a captured CUDA graph)."""
+
+    def __init__(self, ctx: Context, scenes):
+        self.scenes = list(scenes)
+        arr = (C.c_void_p * len(self.scenes))(*[s.handle.value for s in self.scenes])
+        h = C.c_void_p()
+        check(lib().rt_batch_create(ctx.handle, arr, len(self.scenes), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().rt_batch_destroy(self._h)
+            self._h = C.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_items(self, ray_begin, item_scene) -> None:
+        rb = np.ascontiguousarray(ray_begin, np.uint32)
+        it = np.ascontiguousarray(item_scene, np.uint32)
+        check(lib().rt_batch_set_items(self._h, rb.ctypes.data, it.ctypes.data, len(it)))
+
+    def set_tuning(self, **kw) -> None:
+        t = Tuning(*[kw.get(k, 0) for k, _ in Tuning._fields_])
+        check(lib().rt_batch_set_tuning(self._h, C.byref(t)))
+
+    def trace(self, rays, hits, mode: int = MODE_PLAIN, flags=None, default_flags: int = RAY_FLAG_OPAQUE,
+              stream: int = 0) -> None:
+        check(lib().rt_trace_batch(self._h, ptr(rays), ptr(flags), default_flags, mode, ptr(hits), C.c_void_p(stream)))
+
+    def capture(self, rays, hits, mode: int = MODE_PLAIN, flags=None, default_flags: int = RAY_FLAG_OPAQUE,
+                stream: int = 0) -> None:
+        check(lib().rt_batch_graph_capture(self._h, ptr(rays), ptr(flags), default_flags, mode, ptr(hits),
+                                           C.c_void_p(stream)))
+
+    def replay(self, stream: int = 0) -> None:
+        check(lib().rt_batch_graph_launch(self._h, C.c_void_p(stream)))

@@ -52,7 +52,7 @@ class TreeletInfo(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("staged_threads", C.c_uint32), ("staged_epoch", C.c_uint32),
                 ("staged_slots", C.c_uint32), ("refill_lanes", C.c_uint32), ("staged_slot_bytes", C.c_uint32),
-                ("staged_min_votes", C.c_uint32)]
+                ("staged_min_votes", C.c_uint32), ("stack_depth", C.c_uint32)]
 
 
 class TraceStats(C.Structure):
@@ -105,6 +105,13 @@ PROTOTYPES = {
     "rt_partition_remap": (C.c_int, [vp, C.c_uint32, vp]),
     "rt_partition_free": (None, [vp]),
     "rt_trace_host_noalloc": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
+    "rt_batch_create": (C.c_int, [vp, C.POINTER(vp), C.c_uint32, C.POINTER(vp)]),
+    "rt_batch_destroy": (C.c_int, [vp]),
+    "rt_batch_set_items": (C.c_int, [vp, vp, vp, C.c_uint32]),
+    "rt_batch_set_tuning": (C.c_int, [vp, C.POINTER(Tuning)]),
+    "rt_trace_batch": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp]),
+    "rt_batch_graph_capture": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp]),
+    "rt_batch_graph_launch": (C.c_int, [vp, vp]),
 }
 
 _lib = None
