@@ -165,11 +165,35 @@ void free_treelets(rt_scene* s) {
 // Blocks for a persistent launch: as many as fit on the device at once (no
 // more than the rays need).
 uint32_t persistent_grid(const void* kern, uint32_t threads, uint32_t n, size_t dyn_smem = 0) {
-  int dev = 0, sms = 0, per_sm = 0;
+  // occupancy per (device, kernel, block, shared memory), computed once
+  struct Key {
+    int dev;
+    const void* kern;
+    uint32_t threads;
+    size_t smem;
+    bool operator==(const Key& o) const {
+      return dev == o.dev && kern == o.kern && threads == o.threads && smem == o.smem;
+    }
+  };
+  static std::mutex mu;
+  static std::vector<std::pair<Key, uint64_t>> cache;
+  int dev = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)threads, dyn_smem);
-  const uint64_t full = (uint64_t)std::max(1, sms) * (uint64_t)std::max(1, per_sm);
+  const Key key{dev, kern, threads, dyn_smem};
+  uint64_t full = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto& kv : cache)
+      if (kv.first == key) full = kv.second;
+  }
+  if (!full) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)threads, dyn_smem);
+    full = (uint64_t)std::max(1, sms) * (uint64_t)std::max(1, per_sm);
+    std::lock_guard<std::mutex> lock(mu);
+    cache.emplace_back(key, full);
+  }
   const uint64_t need = ((uint64_t)n + threads - 1) / threads;
   return (uint32_t)std::max<uint64_t>(1, std::min(full, need));
 }
