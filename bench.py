@@ -540,6 +540,80 @@ def run_batch(args) -> None:
     batch.close()
 
 
+def run_learned(args) -> None:
+    """The learned prefetcher on a 262,144-triangle unit-cube scene (a
+    config-3 scene): trained on the treelet transitions of 8 jitter seeds of
+    512x512 primary + bounce rays, evaluated on 2 held-out seeds; then the
+    staged traversal voting with the network's hints against the heuristic
+    vote, hits compared bit for bit."""
+    import torch
+
+    import treelet_rt as rt
+    from treelet_rt import learned as L
+    from treelet_rt.autotune import time_trace
+
+    rt.lib()
+    t0 = time.time()
+    blob = rt.Blob.gen(rt.SCENE_CUBE, 262144, 11)
+    ctx = rt.Context(0)
+    scene = rt.Scene(ctx, blob)
+    info = scene.form_treelets(BUDGET)
+    n_tl = info["n_treelets"]
+    cam = rt.default_camera(rt.SCENE_CUBE)
+    train = L.gather_transitions(scene, cam, range(1, 9))
+    test = L.gather_transitions(scene, cam, range(101, 103))
+    t_data = time.time() - t0
+    pop = L.popularity_table(train, n_tl)
+    mlp = L.Mlp(ctx, n_tl, seed=5)
+    t1 = time.time()
+    losses = L.train(mlp, train, steps=args.train_steps, batch=4096, lr=3e-3, lr_final=3e-4)
+    torch.cuda.synchronize()
+    t_train = time.time() - t1
+    pred = L.predict(mlp, test)
+    h_pop = L.hit_rates(pop[test["current"]], test["target"])
+    h_mlp = L.hit_rates(pred, test["target"])
+    h_mix = L.hit_rates(L.combine(pred, pop[test["current"]]), test["target"])
+    hints = L.hint_table(mlp, train, n_tl)
+    prim = rt.camera_rays(cam, 1024, 1024, 1, 201, 1e-4, 1e30)
+    n = len(prim)
+    dp = torch.from_numpy(prim.view(np.uint8)).cuda()
+    hp = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+    db = torch.empty(n * 32, dtype=torch.uint8, device="cuda")
+    scene.trace(dp, hp, rt.MODE_PLAIN, n=n)
+    scene.bounce(dp, hp, db, seed=1201, n=n)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    staged = {}
+    for name, rays_d in (("primary", dp), ("bounce", db)):
+        ref = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+        hh = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+        scene.trace(rays_d, ref, rt.MODE_TREELET, n=n)
+        apply_tuning(scene, "staged", name)
+        row = {}
+        for label, h in (("heuristic_vote", None), ("learned_hints", hints)):
+            scene.set_stage_hints(h)
+            ms = time_trace(scene, rays_d, hh, n, rt.MODE_STAGED, max(3, args.steps), flush)
+            st = scene.stats()
+            row[label] = {"mrays_s": round(n / ms / 1e3, 3),
+                          "smem_read_fraction": round(st["smem_reads"] / max(1, st["smem_reads"] + st["gmem_reads"]), 4),
+                          "hits_equal_treelet_order": bool(torch.equal(hh, ref))}
+        scene.set_stage_hints(None)
+        row["plain_mrays_s"] = round(n / time_trace(scene, rays_d, hh, n, rt.MODE_PLAIN, max(3, args.steps), flush) / 1e3, 3)
+        staged[name] = row
+    line = {"metric": "next-treelet prefetch hit rate, learned vs heuristic (held-out seeds)", "unit": "fraction",
+            "value": round(h_mix[1], 4), "higher_is_better": True, "n_gpus": 1,
+            "config": {"workload": "262,144-triangle unit-cube scene, 8 KiB treelets; MLP 22-64-64-n_treelets "
+                                   "(GELU, BF16 weights, FP32 accumulate)",
+                       "n_treelets": n_tl, "train_transitions": len(train), "test_transitions": len(test),
+                       "train_steps": args.train_steps, "batch": 4096, "data_s": round(t_data, 1),
+                       "train_s": round(t_train, 1), "final_loss": round(float(np.mean(losses[-100:])), 4)},
+            "hit_rate_top1_top4": {"heuristic": [round(x, 4) for x in h_pop], "mlp": [round(x, 4) for x in h_mlp],
+                                   "mlp_with_heuristic_fallback": [round(x, 4) for x in h_mix]},
+            "staged": staged, "dtype": "bf16 (MLP), f32 (traversal)", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+    mlp.close()
+    scene.close()
+
+
 def C_void(v: int):
     import ctypes
 
@@ -556,10 +630,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="small: the same scene with 512x512x1 primary rays + bounces (profiling case)")
-    ap.add_argument("--workload", default="terrain", choices=["terrain", "ao", "batch"],
-                    help="terrain: the headline line; ao: AO budget sweep; batch: many scenes in one launch")
+    ap.add_argument("--workload", default="terrain", choices=["terrain", "ao", "batch", "learned"],
+                    help="terrain: the headline line; ao: AO budget sweep; batch: many scenes in one launch; "
+                         "learned: the learned prefetcher against the heuristic")
     ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--train-steps", type=int, default=6000)
     args = ap.parse_args()
+    if args.workload == "learned" and args.impl != "reference":
+        return run_learned(args)
     if args.workload == "ao" and args.impl != "reference":
         return run_ao(args)
     if args.workload == "batch" and args.impl != "reference":

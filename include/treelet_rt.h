@@ -255,6 +255,15 @@ rt_status rt_trace_host(rt_scene* scene, const rt_ray* rays, const uint32_t* fla
 rt_status rt_trace_host_noalloc(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                                 uint32_t n, uint32_t mode, rt_hit* hits);
 
+/* Predicted next treelets for RT_MODE_STAGED (no reference counterpart):
+ * hints[8 * t + octant] is the dense treelet expected after dense treelet t
+ * for rays whose direction falls in the octant (bit 0: x > 0, bit 1: y > 0,
+ * bit 2: z > 0).  With hints set, a warp stages the treelet its lanes are
+ * predicted to reach after their next one instead of the next one itself.
+ * NULL clears them.  Host array of 8 x n_treelets entries; staging never
+ * changes a result. */
+rt_status rt_scene_set_stage_hints(rt_scene* scene, const uint32_t* hints);
+
 /* Traversal tuning; 0 keeps the current value.  None of these changes any
  * result, only speed. */
 typedef struct rt_tuning {
@@ -307,6 +316,42 @@ rt_status rt_trace_batch(rt_batch* b, const rt_ray* rays, const uint32_t* flags,
 rt_status rt_batch_graph_capture(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                                  uint32_t mode, rt_hit* hits, void* stream);
 rt_status rt_batch_graph_launch(rt_batch* b, void* stream);
+
+/* ---------------- learned treelet predictor ---------------- */
+
+/* No reference counterpart: a small MLP that predicts the treelet a ray
+ * enters after its current one, trained on the traversal's own treelet
+ * traces, used to pick treelets to stage before the rays reach them.
+ *   input  : ray origin (3), direction (3), a 16-dim embedding of the current treelet
+ *   hidden : 64 -> GELU -> 64 -> GELU (BF16 weights, FP32 accumulate)
+ *   output : one logit per treelet of the scene
+ * Training runs on the GPU (forward, softmax cross-entropy, backward, Adam). */
+typedef struct rt_mlp_sample {
+  float origin[3];
+  float dir[3];
+  uint32_t current; /* dense treelet index (rank of its root in rt_treelets_get's roots) */
+  uint32_t target;  /* dense index of the next treelet (ignored by rt_mlp_topk) */
+} rt_mlp_sample;    /* 32 bytes */
+
+#define RT_MLP_HIDDEN 64u
+#define RT_MLP_EMBED 16u
+#define RT_MLP_MAX_BATCH 4096u
+
+typedef struct rt_mlp rt_mlp;
+rt_status rt_mlp_create(rt_ctx* ctx, uint32_t n_treelets, uint64_t seed, rt_mlp** out);
+rt_status rt_mlp_destroy(rt_mlp* m);
+/* Parameter count and host copies (FP32 master values), in the order
+ * E[n_treelets][16], W1[22][64], b1[64], W2[64][64], b2[64], W3[64][n], b3[n]. */
+rt_status rt_mlp_num_params(const rt_mlp* m, uint64_t* n);
+rt_status rt_mlp_get_params(const rt_mlp* m, float* host);
+rt_status rt_mlp_set_params(rt_mlp* m, const float* host);
+/* Mean cross-entropy and its gradient (same order as the parameters) on a
+ * device batch of n <= RT_MLP_MAX_BATCH samples, without updating; grads may be NULL. */
+rt_status rt_mlp_loss_grad(rt_mlp* m, const rt_mlp_sample* samples, uint32_t n, float* loss, float* grads_host);
+/* One Adam step (lr, beta1 0.9, beta2 0.999) on a device batch; *loss receives the batch loss. */
+rt_status rt_mlp_train_step(rt_mlp* m, const rt_mlp_sample* samples, uint32_t n, float lr, float* loss);
+/* Top-4 treelets per sample, highest logit first (device output, n x 4). */
+rt_status rt_mlp_topk(rt_mlp* m, const rt_mlp_sample* samples, uint32_t n, uint32_t* top4);
 
 /* ---------------- treelet-prefetch decision ---------------- */
 

@@ -91,10 +91,6 @@ bool validate_blob(const uint8_t* b, uint64_t n, std::string* err) {
 
 }  // namespace rti
 
-struct rt_ctx {
-  int device = 0;
-};
-
 struct rt_scene {
   rt_ctx* ctx = nullptr;
   std::vector<uint8_t> host_blob;
@@ -110,6 +106,7 @@ struct rt_scene {
   uint32_t* d_roots = nullptr;
   unsigned long long* d_member_first = nullptr;
   uint16_t* d_member_bytes = nullptr;
+  uint32_t* d_hint = nullptr;  // staged-mode predictions (8 per treelet) or null
   uint32_t slot_bytes = 0;
   // per-launch counters and status (library scratch)
   unsigned long long* d_stats = nullptr;
@@ -153,6 +150,8 @@ void free_treelets(rt_scene* s) {
   cudaFree(s->d_roots);
   cudaFree(s->d_member_first);
   cudaFree(s->d_member_bytes);
+  cudaFree(s->d_hint);
+  s->d_hint = nullptr;
   s->d_meta = nullptr;
   s->d_images = nullptr;
   s->d_image_off = nullptr;
@@ -490,7 +489,22 @@ rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint3
   a.stats = s->d_stats;
   a.status = s->d_status;
   a.queue = s->d_queue;
+  a.hint = s->d_hint;
   return launch_trace(a, mode, s->tuning, s->slot_bytes, st);
+}
+
+rt_status rt_scene_set_stage_hints(rt_scene* s, const uint32_t* hints) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_scene_set_stage_hints: NULL scene");
+  if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_scene_set_stage_hints: call rt_treelets_form first");
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  cudaFree(s->d_hint);
+  s->d_hint = nullptr;
+  if (!hints) return RT_OK;
+  const size_t n = (size_t)s->part.roots.size() * 8;
+  rt_status st = dalloc(&s->d_hint, sizeof(uint32_t) * n);
+  if (st != RT_OK) return st;
+  RT_CUDA(cudaMemcpy(s->d_hint, hints, sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+  return RT_OK;
 }
 
 rt_status rt_trace_stats_get(rt_scene* s, rt_trace_stats* out) {

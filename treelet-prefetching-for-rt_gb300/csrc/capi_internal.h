@@ -13,6 +13,10 @@ struct rt_blob {
   std::vector<uint8_t> bytes;
 };
 
+struct rt_ctx {
+  int device = 0;
+};
+
 namespace rti {
 
 void set_error(const std::string& msg);

@@ -1,0 +1,544 @@
+// The learned treelet predictor: forward, softmax cross-entropy, backward,
+// Adam and top-4, all on the GPU.
+//
+//   x  = [origin(3), dir(3), E[current](16)]           22 inputs (padded to 32)
+//   h1 = GELU(x W1 + b1)                                64
+//   h2 = GELU(h1 W2 + b2)                               64
+//   z  = h2 W3 + b3                                     one logit per treelet
+//
+// Weights are used in BF16 with FP32 accumulation; FP32 master copies are
+// what Adam updates.  The matrix products run on the tensor cores through
+// mma.sync m16n8k16 (BF16 in, FP32 accumulate): every product here has one
+// dimension of 64 or less, which the warp-level MMA covers without the
+// shared-memory staging and TMEM round trip a tcgen05 tile would need.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "capi_internal.h"
+
+namespace {
+
+constexpr int H = RT_MLP_HIDDEN;  // 64
+constexpr int EMB = RT_MLP_EMBED; // 16
+constexpr int XIN = 22;           // real inputs
+constexpr int XP = 32;            // padded input width
+using bf16 = __nv_bfloat16;
+
+// ----------------------------------------------------------------- GEMM
+// C[M x N] (+)= A[M x K] * B[K x N].  A is read row-major (AT = false:
+// A[m * lda + k]) or transposed (AT = true: A[k * lda + m]); B is read
+// row-major (BT = false: B[k * ldb + n]) or transposed (BT = true:
+// B[n * ldb + k]).  64 x 64 CTA tile, 4 warps of 32 x 32, K in steps of 32;
+// gridDim.z splits K, partial sums are added atomically (EPI_ACC).
+enum Epi { EPI_STORE = 0, EPI_ACC = 1, EPI_BIAS_GELU = 2, EPI_BIAS = 3 };
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.3989422804014327f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+__device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+template <bool AT, bool BT, int EPI>
+__global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const bf16* __restrict__ A, int lda,
+                                                   const bf16* __restrict__ B, int ldb, float* __restrict__ C,
+                                                   int ldc, const float* __restrict__ bias, bf16* __restrict__ Hout) {
+  constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
+  __shared__ __align__(16) bf16 As[BM][BK + PAD];
+  __shared__ __align__(16) bf16 Bs[BN][BK + PAD];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  // K range of this split
+  const int splits = gridDim.z;
+  const int kchunk = ((K + splits * BK - 1) / (splits * BK)) * BK;
+  const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0f;
+  const bf16 zero = __float2bfloat16(0.0f);
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    for (int e = tid; e < BM * BK; e += 128) {
+      const int r = e / BK, c = e % BK;
+      const int m = m0 + r, k = k0 + c;
+      bf16 v = zero;
+      if (m < M && k < kend) v = AT ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+      As[r][c] = v;
+    }
+    for (int e = tid; e < BN * BK; e += 128) {
+      const int r = e / BK, c = e % BK;
+      const int n = n0 + r, k = k0 + c;
+      bf16 v = zero;
+      if (n < N && k < kend) v = BT ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
+      Bs[r][c] = v;
+    }
+    __syncthreads();
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int rb = wm + i * 16;
+        af[i][0] = *reinterpret_cast<const uint32_t*>(&As[rb + g][kk + 2 * t]);
+        af[i][1] = *reinterpret_cast<const uint32_t*>(&As[rb + g + 8][kk + 2 * t]);
+        af[i][2] = *reinterpret_cast<const uint32_t*>(&As[rb + g][kk + 2 * t + 8]);
+        af[i][3] = *reinterpret_cast<const uint32_t*>(&As[rb + g + 8][kk + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int nb = wn + j * 8;
+        bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[nb + g][kk + 2 * t]);
+        bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[nb + g][kk + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          asm volatile(
+              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+              "{%0,%1,%2,%3};\n"
+              : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
+              : "r"(af[i][0]), "r"(af[i][1]), "r"(af[i][2]), "r"(af[i][3]), "r"(bfr[j][0]), "r"(bfr[j][1]));
+    }
+    __syncthreads();
+  }
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int m = m0 + wm + i * 16 + g + (r >= 2 ? 8 : 0);
+        const int n = n0 + wn + j * 8 + 2 * t + (r & 1);
+        if (m >= M || n >= N) continue;
+        float v = acc[i][j][r];
+        float* dst = C + (size_t)m * ldc + n;
+        if (EPI == EPI_ACC) {
+          atomicAdd(dst, v);
+        } else if (EPI == EPI_STORE) {
+          *dst = v;
+        } else {
+          v += bias[n];
+          *dst = v;
+          if (EPI == EPI_BIAS_GELU) Hout[(size_t)m * ldc + n] = __float2bfloat16(gelu(v));
+        }
+      }
+}
+
+template <bool AT, bool BT, int EPI>
+void gemm(int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc, const float* bias,
+          bf16* Hout, int splits, cudaStream_t st) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64, splits);
+  gemm_kernel<AT, BT, EPI><<<grid, 128, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, Hout);
+}
+
+// ------------------------------------------------------------ elementwise
+// A sample whose current treelet is out of range gets a zero embedding.
+__global__ void gather_inputs(const rt_mlp_sample* __restrict__ s, int n, const bf16* __restrict__ E, uint32_t C,
+                              bf16* __restrict__ X) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * XP) return;
+  const int b = i / XP, c = i % XP;
+  float v = 0.0f;
+  if (c < 3) v = s[b].origin[c];
+  else if (c < 6) v = s[b].dir[c - 3];
+  else if (c < XIN) {
+    const uint32_t cur = s[b].current;
+    X[i] = cur < C ? E[(size_t)cur * EMB + (c - 6)] : __float2bfloat16(0.0f);
+    return;
+  }
+  X[i] = __float2bfloat16(v);
+}
+
+// Per row: loss += (logsumexp(z) - z[target]) / n; dZ = (softmax(z) - onehot) / n.
+__global__ void softmax_xent(const float* __restrict__ Z, int n, int C, const rt_mlp_sample* __restrict__ s,
+                             bf16* __restrict__ dZ, float* __restrict__ loss) {
+  const int row = blockIdx.x;
+  const float* z = Z + (size_t)row * C;
+  __shared__ float red[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  float mx = -INFINITY;
+  for (int j = tid; j < C; j += blockDim.x) mx = fmaxf(mx, z[j]);
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) red[warp] = mx;
+  __syncthreads();
+  mx = red[0];
+  for (int w = 1; w < nw; ++w) mx = fmaxf(mx, red[w]);
+  __syncthreads();
+  float sum = 0.0f;
+  for (int j = tid; j < C; j += blockDim.x) sum += expf(z[j] - mx);
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) red[warp] = sum;
+  __syncthreads();
+  sum = 0.0f;
+  for (int w = 0; w < nw; ++w) sum += red[w];
+  const uint32_t tgt = s[row].target;
+  const float inv = 1.0f / sum, scale = 1.0f / (float)n;
+  if (dZ) {
+    bf16* d = dZ + (size_t)row * C;
+    for (int j = tid; j < C; j += blockDim.x) {
+      const float p = expf(z[j] - mx) * inv;
+      d[j] = __float2bfloat16((p - (j == (int)tgt ? 1.0f : 0.0f)) * scale);
+    }
+  }
+  if (tid == 0 && tgt < (uint32_t)C) atomicAdd(loss, (logf(sum) + mx - z[tgt]) * scale);
+}
+
+// dZ = dH * GELU'(Z) as BF16.
+__global__ void gelu_back(const float* __restrict__ dH, const float* __restrict__ Z, bf16* __restrict__ dZ, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dZ[i] = __float2bfloat16(dH[i] * gelu_grad(Z[i]));
+}
+
+// out[c] = sum_r X[r][c]
+__global__ void col_sum(const bf16* __restrict__ X, int rows, int cols, float* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.0f;
+  for (int r = 0; r < rows; ++r) s += __bfloat162float(X[(size_t)r * cols + c]);
+  out[c] = s;
+}
+
+__global__ void embed_grad(const float* __restrict__ dX, const rt_mlp_sample* __restrict__ s, int n, uint32_t C,
+                           float* __restrict__ gE) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * EMB) return;
+  const int b = i / EMB, j = i % EMB;
+  const uint32_t cur = s[b].current;
+  if (cur < C) atomicAdd(gE + (size_t)cur * EMB + j, dX[(size_t)b * XP + 6 + j]);
+}
+
+__global__ void copy_rows(const float* __restrict__ src, int src_ld, float* __restrict__ dst, int rows, int cols) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < rows * cols) dst[i] = src[(size_t)(i / cols) * src_ld + (i % cols)];
+}
+
+__global__ void adam(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v, const float* __restrict__ g,
+                     uint64_t n, float lr, float c1, float c2) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = 0.9f * m[i] + 0.1f * gi;
+  const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+}
+
+__global__ void to_bf16(const float* __restrict__ src, bf16* __restrict__ dst, uint64_t n) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = __float2bfloat16(src[i]);
+}
+
+// W1 (22 x 64) -> padded BF16 (32 x 64, rows 22..31 zero)
+__global__ void w1_to_bf16(const float* __restrict__ w1, bf16* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < XP * H) dst[i] = __float2bfloat16(i < XIN * H ? w1[i] : 0.0f);
+}
+
+// Deterministic initial values from a hash of (seed, index).
+__global__ void init_params(float* __restrict__ p, uint64_t n, uint64_t seed, uint64_t offW1, uint64_t offb1,
+                            uint64_t offW2, uint64_t offb2, uint64_t offW3, uint64_t offb3) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t h = rti::pcg_hash((uint32_t)i ^ rti::pcg_hash((uint32_t)seed));
+  h = rti::pcg_hash(h ^ (uint32_t)(i >> 32));
+  const float u = ((float)(h >> 8) * (1.0f / 16777216.0f)) * 2.0f - 1.0f;  // [-1, 1)
+  float v;
+  if (i < offW1) v = 0.1f * u;                       // embedding
+  else if (i < offb1) v = u * 0.2132f;               // W1: 1/sqrt(22)
+  else if (i < offW2) v = 0.0f;
+  else if (i < offb2) v = u * 0.125f;                // W2: 1/sqrt(64)
+  else if (i < offW3) v = 0.0f;
+  else if (i < offb3) v = u * 0.125f;                // W3
+  else v = 0.0f;
+  p[i] = v;
+}
+
+// One warp per row: the four largest logits (ties: lower index first).
+__global__ void topk4(const float* __restrict__ Z, int n, int C, uint32_t* __restrict__ out) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* z = Z + (size_t)row * C;
+  float v[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  int ix[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+  for (int j = lane; j < C; j += 32) {
+    const float x = z[j];
+    if (x > v[3] || (x == v[3] && j < ix[3])) {
+      int p = 3;
+      while (p > 0 && (x > v[p - 1] || (x == v[p - 1] && j < ix[p - 1]))) {
+        v[p] = v[p - 1];
+        ix[p] = ix[p - 1];
+        --p;
+      }
+      v[p] = x;
+      ix[p] = j;
+    }
+  }
+  int head = 0;
+  for (int k = 0; k < 4; ++k) {
+    float bv = head < 4 ? v[head] : -INFINITY;
+    int bi = head < 4 ? ix[head] : 0x7fffffff;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (head < 4 && ix[head] == bi) ++head;
+    if (lane == 0) out[(size_t)row * 4 + k] = (uint32_t)(bi == 0x7fffffff ? 0xFFFFFFFFu : bi);
+  }
+}
+
+}  // namespace
+
+struct rt_mlp {
+  int device = 0;
+  uint32_t C = 0;
+  uint64_t n_params = 0, offW1 = 0, offb1 = 0, offW2 = 0, offb2 = 0, offW3 = 0, offb3 = 0;
+  float *P = nullptr, *M = nullptr, *V = nullptr, *G = nullptr;
+  bf16 *E16 = nullptr, *W1_16 = nullptr, *W2_16 = nullptr, *W3_16 = nullptr;
+  bf16 *X = nullptr, *H1 = nullptr, *H2 = nullptr, *dZ3 = nullptr, *dZ2 = nullptr, *dZ1 = nullptr;
+  float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *dH2 = nullptr, *dH1 = nullptr, *dX = nullptr, *dW1 = nullptr;
+  float* loss = nullptr;
+  uint64_t step = 0;
+  cudaStream_t st = nullptr;
+};
+
+namespace {
+
+rt_status cfail(cudaError_t e, const char* what) {
+  return rti::fail(RT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define MLP_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cfail(e_, #call);     \
+  } while (0)
+
+template <class T>
+cudaError_t mk(T** p, size_t count) {
+  return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+}
+
+unsigned blocks(uint64_t n, unsigned t = 256) { return (unsigned)((n + t - 1) / t); }
+
+void refresh_bf16(rt_mlp* m) {
+  to_bf16<<<blocks((uint64_t)m->C * EMB), 256, 0, m->st>>>(m->P, m->E16, (uint64_t)m->C * EMB);
+  w1_to_bf16<<<blocks(XP * H), 256, 0, m->st>>>(m->P + m->offW1, m->W1_16);
+  to_bf16<<<blocks(H * H), 256, 0, m->st>>>(m->P + m->offW2, m->W2_16, H * H);
+  to_bf16<<<blocks((uint64_t)H * m->C), 256, 0, m->st>>>(m->P + m->offW3, m->W3_16, (uint64_t)H * m->C);
+}
+
+int ksplit(int K, int tiles) {
+  // enough CTAs to cover the GPU when the output has few tiles
+  int s = 1;
+  while (tiles * s < 304 && K / (s * 2) >= 256) s *= 2;
+  return s;
+}
+
+// Forward (and, when grads is true, backward into G) for n samples.
+rt_status run(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, bool grads, bool loss_only_logits) {
+  const int B = (int)n, C = (int)m->C;
+  cudaStream_t st = m->st;
+  gather_inputs<<<blocks((uint64_t)B * XP), 256, 0, st>>>(s, B, m->E16, m->C, m->X);
+  gemm<false, false, EPI_BIAS_GELU>(B, H, XP, m->X, XP, m->W1_16, H, m->Z1, H, m->P + m->offb1, m->H1, 1, st);
+  gemm<false, false, EPI_BIAS_GELU>(B, H, H, m->H1, H, m->W2_16, H, m->Z2, H, m->P + m->offb2, m->H2, 1, st);
+  gemm<false, false, EPI_BIAS>(B, C, H, m->H2, H, m->W3_16, C, m->Z3, C, m->P + m->offb3, nullptr, 1, st);
+  if (loss_only_logits) return RT_OK;
+  MLP_CUDA(cudaMemsetAsync(m->loss, 0, sizeof(float), st));
+  softmax_xent<<<B, 256, 0, st>>>(m->Z3, B, C, s, grads ? m->dZ3 : nullptr, m->loss);
+  if (!grads) return RT_OK;
+  MLP_CUDA(cudaMemsetAsync(m->G, 0, sizeof(float) * m->n_params, st));
+  // W3, b3
+  gemm<true, false, EPI_ACC>(H, C, B, m->H2, H, m->dZ3, C, m->G + m->offW3, C, nullptr, nullptr,
+                             ksplit(B, (C + 63) / 64), st);
+  col_sum<<<blocks(C), 256, 0, st>>>(m->dZ3, B, C, m->G + m->offb3);
+  // dH2 = dZ3 W3^T
+  MLP_CUDA(cudaMemsetAsync(m->dH2, 0, sizeof(float) * B * H, st));
+  gemm<false, true, EPI_ACC>(B, H, C, m->dZ3, C, m->W3_16, C, m->dH2, H, nullptr, nullptr,
+                             ksplit(C, (B + 63) / 64), st);
+  gelu_back<<<blocks((uint64_t)B * H), 256, 0, st>>>(m->dH2, m->Z2, m->dZ2, B * H);
+  // W2, b2
+  gemm<true, false, EPI_ACC>(H, H, B, m->H1, H, m->dZ2, H, m->G + m->offW2, H, nullptr, nullptr, ksplit(B, 1), st);
+  col_sum<<<1, H, 0, st>>>(m->dZ2, B, H, m->G + m->offb2);
+  // dH1 = dZ2 W2^T
+  MLP_CUDA(cudaMemsetAsync(m->dH1, 0, sizeof(float) * B * H, st));
+  gemm<false, true, EPI_ACC>(B, H, H, m->dZ2, H, m->W2_16, H, m->dH1, H, nullptr, nullptr, 1, st);
+  gelu_back<<<blocks((uint64_t)B * H), 256, 0, st>>>(m->dH1, m->Z1, m->dZ1, B * H);
+  // W1 (first 22 rows of the padded product), b1
+  MLP_CUDA(cudaMemsetAsync(m->dW1, 0, sizeof(float) * XP * H, st));
+  gemm<true, false, EPI_ACC>(XP, H, B, m->X, XP, m->dZ1, H, m->dW1, H, nullptr, nullptr, ksplit(B, 1), st);
+  copy_rows<<<blocks(XIN * H), 256, 0, st>>>(m->dW1, H, m->G + m->offW1, XIN, H);
+  col_sum<<<1, H, 0, st>>>(m->dZ1, B, H, m->G + m->offb1);
+  // dX = dZ1 W1^T -> embedding rows
+  MLP_CUDA(cudaMemsetAsync(m->dX, 0, sizeof(float) * B * XP, st));
+  gemm<false, true, EPI_ACC>(B, XP, H, m->dZ1, H, m->W1_16, H, m->dX, XP, nullptr, nullptr, 1, st);
+  embed_grad<<<blocks((uint64_t)B * EMB), 256, 0, st>>>(m->dX, s, B, m->C, m->G);
+  return RT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rt_status rt_mlp_create(rt_ctx* ctx, uint32_t n_treelets, uint64_t seed, rt_mlp** out) {
+  if (!ctx || !out || n_treelets == 0) return rti::fail(RT_ERR_INVALID, "rt_mlp_create: bad argument");
+  if (n_treelets > (1u << 24)) return rti::fail(RT_ERR_TOO_LARGE, "rt_mlp_create: at most 16M treelets");
+  *out = nullptr;
+  MLP_CUDA(cudaSetDevice(ctx->device));
+  auto* m = new rt_mlp();
+  m->device = ctx->device;
+  const uint64_t C = n_treelets;
+  m->C = n_treelets;
+  m->offW1 = C * EMB;
+  m->offb1 = m->offW1 + XIN * H;
+  m->offW2 = m->offb1 + H;
+  m->offb2 = m->offW2 + H * H;
+  m->offW3 = m->offb2 + H;
+  m->offb3 = m->offW3 + H * C;
+  m->n_params = m->offb3 + C;
+  const size_t MB = RT_MLP_MAX_BATCH;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  chk(mk(&m->P, m->n_params));
+  chk(mk(&m->M, m->n_params));
+  chk(mk(&m->V, m->n_params));
+  chk(mk(&m->G, m->n_params));
+  chk(mk(&m->E16, C * EMB));
+  chk(mk(&m->W1_16, XP * H));
+  chk(mk(&m->W2_16, H * H));
+  chk(mk(&m->W3_16, H * C));
+  chk(mk(&m->X, MB * XP));
+  chk(mk(&m->H1, MB * H));
+  chk(mk(&m->H2, MB * H));
+  chk(mk(&m->dZ3, MB * C));
+  chk(mk(&m->dZ2, MB * H));
+  chk(mk(&m->dZ1, MB * H));
+  chk(mk(&m->Z1, MB * H));
+  chk(mk(&m->Z2, MB * H));
+  chk(mk(&m->Z3, MB * C));
+  chk(mk(&m->dH2, MB * H));
+  chk(mk(&m->dH1, MB * H));
+  chk(mk(&m->dX, MB * XP));
+  chk(mk(&m->dW1, XP * H));
+  chk(mk(&m->loss, 1));
+  chk(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
+  if (e != cudaSuccess) {
+    rt_mlp_destroy(m);
+    return rti::fail(RT_ERR_OOM, std::string("rt_mlp_create: ") + cudaGetErrorString(e));
+  }
+  init_params<<<blocks(m->n_params), 256, 0, m->st>>>(m->P, m->n_params, seed, m->offW1, m->offb1, m->offW2,
+                                                         m->offb2, m->offW3, m->offb3);
+  cudaMemsetAsync(m->M, 0, sizeof(float) * m->n_params, m->st);
+  cudaMemsetAsync(m->V, 0, sizeof(float) * m->n_params, m->st);
+  refresh_bf16(m);
+  e = cudaStreamSynchronize(m->st);
+  if (e != cudaSuccess) {
+    rt_mlp_destroy(m);
+    return cfail(e, "rt_mlp_create");
+  }
+  *out = m;
+  return RT_OK;
+}
+
+rt_status rt_mlp_destroy(rt_mlp* m) {
+  if (!m) return RT_OK;
+  cudaSetDevice(m->device);
+  void* ptrs[] = {m->P, m->M, m->V, m->G, m->E16, m->W1_16, m->W2_16, m->W3_16, m->X, m->H1, m->H2, m->dZ3,
+                  m->dZ2, m->dZ1, m->Z1, m->Z2, m->Z3, m->dH2, m->dH1, m->dX, m->dW1, m->loss};
+  for (void* p : ptrs) cudaFree(p);
+  if (m->st) cudaStreamDestroy(m->st);
+  delete m;
+  return RT_OK;
+}
+
+rt_status rt_mlp_num_params(const rt_mlp* m, uint64_t* n) {
+  if (!m || !n) return rti::fail(RT_ERR_INVALID, "rt_mlp_num_params: NULL");
+  *n = m->n_params;
+  return RT_OK;
+}
+
+rt_status rt_mlp_get_params(const rt_mlp* m, float* host) {
+  if (!m || !host) return rti::fail(RT_ERR_INVALID, "rt_mlp_get_params: NULL");
+  MLP_CUDA(cudaSetDevice(m->device));
+  MLP_CUDA(cudaStreamSynchronize(m->st));
+  MLP_CUDA(cudaMemcpy(host, m->P, sizeof(float) * m->n_params, cudaMemcpyDeviceToHost));
+  return RT_OK;
+}
+
+rt_status rt_mlp_set_params(rt_mlp* m, const float* host) {
+  if (!m || !host) return rti::fail(RT_ERR_INVALID, "rt_mlp_set_params: NULL");
+  MLP_CUDA(cudaSetDevice(m->device));
+  MLP_CUDA(cudaStreamSynchronize(m->st));
+  MLP_CUDA(cudaMemcpy(m->P, host, sizeof(float) * m->n_params, cudaMemcpyHostToDevice));
+  refresh_bf16(m);
+  MLP_CUDA(cudaStreamSynchronize(m->st));
+  return RT_OK;
+}
+
+rt_status rt_mlp_loss_grad(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, float* loss, float* grads_host) {
+  if (!m || !s || n == 0) return rti::fail(RT_ERR_INVALID, "rt_mlp_loss_grad: bad argument");
+  if (n > RT_MLP_MAX_BATCH) return rti::fail(RT_ERR_TOO_LARGE, "rt_mlp_loss_grad: batch above RT_MLP_MAX_BATCH");
+  MLP_CUDA(cudaSetDevice(m->device));
+  rt_status st = run(m, s, n, grads_host != nullptr, false);
+  if (st != RT_OK) return st;
+  MLP_CUDA(cudaGetLastError());
+  MLP_CUDA(cudaStreamSynchronize(m->st));
+  if (loss) MLP_CUDA(cudaMemcpy(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost));
+  if (grads_host) MLP_CUDA(cudaMemcpy(grads_host, m->G, sizeof(float) * m->n_params, cudaMemcpyDeviceToHost));
+  return RT_OK;
+}
+
+rt_status rt_mlp_train_step(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, float lr, float* loss) {
+  if (!m || !s || n == 0) return rti::fail(RT_ERR_INVALID, "rt_mlp_train_step: bad argument");
+  if (n > RT_MLP_MAX_BATCH) return rti::fail(RT_ERR_TOO_LARGE, "rt_mlp_train_step: batch above RT_MLP_MAX_BATCH");
+  MLP_CUDA(cudaSetDevice(m->device));
+  rt_status st = run(m, s, n, true, false);
+  if (st != RT_OK) return st;
+  m->step += 1;
+  const float c1 = 1.0f - powf(0.9f, (float)m->step), c2 = 1.0f - powf(0.999f, (float)m->step);
+  adam<<<blocks(m->n_params), 256, 0, m->st>>>(m->P, m->M, m->V, m->G, m->n_params, lr, c1, c2);
+  refresh_bf16(m);
+  MLP_CUDA(cudaGetLastError());
+  if (loss) {
+    MLP_CUDA(cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->st));
+    MLP_CUDA(cudaStreamSynchronize(m->st));
+  }
+  return RT_OK;
+}
+
+rt_status rt_mlp_topk(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, uint32_t* top4) {
+  if (!m || !s || !top4) return rti::fail(RT_ERR_INVALID, "rt_mlp_topk: NULL");
+  MLP_CUDA(cudaSetDevice(m->device));
+  for (uint32_t b0 = 0; b0 < n; b0 += RT_MLP_MAX_BATCH) {
+    const uint32_t nb = std::min<uint32_t>(RT_MLP_MAX_BATCH, n - b0);
+    rt_status st = run(m, s + b0, nb, false, true);
+    if (st != RT_OK) return st;
+    topk4<<<blocks(nb, 8), 256, 0, m->st>>>(m->Z3, (int)nb, (int)m->C, top4 + (size_t)b0 * 4);
+  }
+  MLP_CUDA(cudaGetLastError());
+  MLP_CUDA(cudaStreamSynchronize(m->st));
+  return RT_OK;
+}
+
+}  // extern "C"

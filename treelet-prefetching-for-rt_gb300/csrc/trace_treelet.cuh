@@ -369,6 +369,12 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
       if (st.pending_slot == kNone && !st.disabled) {
         const uint32_t nl = (have && w.active()) ? w.next_loc() : kNone;
         uint32_t key = nl == kNone ? kNone : (nl >> kSlotBitsDev);
+        if (a.hint && key != kNone) {
+          // vote for the treelet predicted to follow the one the ray enters next
+          const uint32_t oct = (w.D.x > 0.0f ? 1u : 0u) | (w.D.y > 0.0f ? 2u : 0u) | (w.D.z > 0.0f ? 4u : 0u);
+          key = __ldg(a.hint + (size_t)key * 8 + oct);
+          if (key >= a.n_treelets) key = kNone;
+        }
         if (key != kNone)
           for (uint32_t s = 0; s < slots; ++s)
             if (st.resident[s] == key) key = kNone;  // already resident

@@ -231,6 +231,15 @@ class Scene:
         check(lib().rt_treelets_remap(self._h, stride, out.ctypes.data))
         return out
 
+    def set_stage_hints(self, hints) -> None:
+        """hints: (n_treelets, 8) uint32 predicted next treelets, or None to clear."""
+        if hints is None:
+            check(lib().rt_scene_set_stage_hints(self._h, None))
+            return
+        h = np.ascontiguousarray(hints, np.uint32)
+        assert h.size == 8 * self.treelet_info["n_treelets"]
+        check(lib().rt_scene_set_stage_hints(self._h, h.ctypes.data))
+
     def set_tuning(self, block_threads=0, staged_threads=0, staged_epoch=0, staged_slots=0, refill_lanes=0,
                    staged_slot_bytes=0, staged_min_votes=0, stack_depth=0) -> None:
         t = Tuning(block_threads, staged_threads, staged_epoch, staged_slots, refill_lanes, staged_slot_bytes,

@@ -112,6 +112,7 @@ PROTOTYPES = {
     "rt_trace_batch": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp]),
     "rt_batch_graph_capture": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp]),
     "rt_batch_graph_launch": (C.c_int, [vp, vp]),
+    "rt_scene_set_stage_hints": (C.c_int, [vp, vp]),
 }
 
 _lib = None

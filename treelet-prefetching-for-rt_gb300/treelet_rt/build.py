@@ -31,7 +31,7 @@ HOST_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-
 NVCC_FLAGS = ["-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off"] + ARCH
 
 HOST_SOURCES = ["builder.cpp", "scenes.cpp", "treelets.cpp", "partition_capi.cpp"]
-CUDA_SOURCES = ["capi.cu", "noalloc.cu"]
+CUDA_SOURCES = ["capi.cu", "noalloc.cu", "mlp.cu"]
 
 
 def _nvcc() -> str:
