@@ -600,7 +600,7 @@ def run_learned(args) -> None:
         row["plain_mrays_s"] = round(n / time_trace(scene, rays_d, hh, n, rt.MODE_PLAIN, max(3, args.steps), flush) / 1e3, 3)
         staged[name] = row
     line = {"metric": "next-treelet prefetch hit rate, learned vs heuristic (held-out seeds)", "unit": "fraction",
-            "value": round(h_mix[1], 4), "higher_is_better": True, "n_gpus": 1,
+            "value": round(h_mlp[1], 4), "higher_is_better": True, "n_gpus": 1,
             "config": {"workload": "262,144-triangle unit-cube scene, 8 KiB treelets; MLP 22-64-64-n_treelets "
                                    "(GELU, BF16 weights, FP32 accumulate)",
                        "n_treelets": n_tl, "train_transitions": len(train), "test_transitions": len(test),

@@ -65,8 +65,19 @@ def lib():
                                    C.c_uint32, C.c_int]
         L.oracle_prefetch_decide.restype = C.c_int
         L.oracle_prefetch_decide.argtypes = [vp, vp, C.c_uint32, C.POINTER(_Params), vp, vp]
+        L.oracle_decode_node.restype = C.c_int
+        L.oracle_decode_node.argtypes = [vp, C.c_uint32, C.c_int, vp]
         _lib = L
     return _lib
+
+
+def decode_node(blob: np.ndarray, unit: int, kind: int) -> np.ndarray:
+    """62 decoded values of one node (layout of oracle/ref_pin/pin_decoders.cpp)."""
+    blob = np.ascontiguousarray(blob, np.uint8)
+    out = np.zeros(62, np.float64)
+    if lib().oracle_decode_node(blob.ctypes.data, unit, kind, out.ctypes.data) != 0:
+        raise OracleError(lib().oracle_last_error().decode())
+    return out
 
 
 class OracleError(RuntimeError):

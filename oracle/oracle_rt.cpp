@@ -179,13 +179,17 @@ constexpr uint32_t TYPE_QUAD = 0;
 
 struct GEN_RT_BVH_QUAD_LEAF {
   GEN_RT_BVH_PRIMITIVE_LEAF_DESCRIPTOR LeafDescriptor;
-  uint32_t PrimitiveIndex0, PrimitiveIndex1Delta;
+  uint32_t PrimitiveIndex0, PrimitiveIndex1Delta, j0, j1, j2;
   float3 QuadVertex[4];
 };
 void unpack_quad(GEN_RT_BVH_QUAD_LEAF* d, const uint8_t* p) {
   unpack_desc(&d->LeafDescriptor, p);
   d->PrimitiveIndex0 = rd<uint32_t>(p + 8);
-  d->PrimitiveIndex1Delta = rd<uint32_t>(p + 12) & 0x0001ffff;
+  const uint32_t t = rd<uint32_t>(p + 12);
+  d->PrimitiveIndex1Delta = t & 0x0001ffff;
+  d->j0 = (t >> 17) & 3;
+  d->j1 = (t >> 19) & 3;
+  d->j2 = (t >> 21) & 3;
   for (int v = 0; v < 4; ++v)
     d->QuadVertex[v] = {rd<float>(p + 16 + 12 * v), rd<float>(p + 20 + 12 * v), rd<float>(p + 24 + 12 * v)};
 }
@@ -840,6 +844,60 @@ void trace_range(const uint8_t* blob, const oracle_treelets* tl, const rt_ray* r
 }  // namespace
 
 extern "C" {
+
+// One node decoded by the oracle's decoders, in the record layout of
+// oracle/ref_pin/pin_decoders.cpp (which decodes with the reference header).
+int oracle_decode_node(const uint8_t* blob, uint32_t unit, int kind, double* out) {
+  const uint8_t* p = blob + (uint64_t)unit * 64;
+  std::vector<double> v;
+  if (kind == 0) {
+    GEN_RT_BVH h;
+    unpack_bvh(&h, p);
+    v = {(double)h.RootNodeOffset, h.BoundsMin.x, h.BoundsMin.y, h.BoundsMin.z, h.BoundsMax.x, h.BoundsMax.y,
+         h.BoundsMax.z};
+  } else if (kind == 1) {
+    GEN_RT_BVH_INTERNAL_NODE n;
+    unpack_internal(&n, p);
+    v = {n.Origin.x, n.Origin.y, n.Origin.z, (double)n.ChildOffset, (double)n.NodeType,
+         (double)n.ChildBoundsExponentX, (double)n.ChildBoundsExponentY, (double)n.ChildBoundsExponentZ,
+         (double)n.NodeRayMask};
+    for (int i = 0; i < 6; ++i) v.push_back(n.ChildSize[i]);
+    for (int i = 0; i < 6; ++i) v.push_back(n.ChildType[i]);
+    for (int i = 0; i < 6; ++i) {
+      float3 lo, hi;
+      set_child_bounds(&n, i, &lo, &hi);
+      v.insert(v.end(), {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z});
+    }
+  } else if (kind == 2) {
+    GEN_RT_BVH_INSTANCE_LEAF l;
+    unpack_instance(&l, p);
+    const float4x4 w2o = instance_leaf_matrix_to_float4x4(l.w2o_run);
+    const float4x4 o2w = instance_leaf_matrix_to_float4x4(l.o2w_run);
+    v = {(double)l.ShaderIndex, (double)l.GeometryRayMask, (double)l.InstanceContributionToHitGroupIndex,
+         (double)l.LeafType, (double)l.GeometryFlags, (double)l.InstanceFlags, (double)l.BVHAddress,
+         (double)l.InstanceID, (double)l.InstanceIndex};
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) v.push_back(w2o.m[a][b]);
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) v.push_back(o2w.m[a][b]);
+    const float4 q = w2o * float4{0.5f, -1.25f, 2.0f, 1.0f};
+    const float4 d = w2o * float4{0.25f, 0.75f, -0.5f, 0.0f};
+    v.insert(v.end(), {q.x, q.y, q.z, q.w, d.x, d.y, d.z, d.w});
+  } else if (kind == 3) {
+    GEN_RT_BVH_QUAD_LEAF q;
+    unpack_quad(&q, p);
+    v = {(double)q.LeafDescriptor.ShaderIndex, (double)q.LeafDescriptor.GeometryRayMask,
+         (double)q.LeafDescriptor.GeometryIndex, (double)q.LeafDescriptor.LeafType,
+         (double)q.LeafDescriptor.GeometryFlags, (double)q.PrimitiveIndex0, (double)q.PrimitiveIndex1Delta,
+         (double)q.j0, (double)q.j1, (double)q.j2};
+    for (int k = 0; k < 4; ++k) v.insert(v.end(), {q.QuadVertex[k].x, q.QuadVertex[k].y, q.QuadVertex[k].z});
+  } else {
+    g_err = "oracle_decode_node: unknown kind";
+    return -1;
+  }
+  for (int i = 0; i < 62; ++i) out[i] = i < (int)v.size() ? v[i] : 0.0;
+  return 0;
+}
 
 const char* oracle_last_error(void) { return g_err.c_str(); }
 

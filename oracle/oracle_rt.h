@@ -23,6 +23,12 @@ extern "C" {
 
 typedef struct oracle_treelets oracle_treelets;
 
+/* One node decoded by the oracle (kind 0 header, 1 internal, 2 instance
+ * leaf, 3 quad leaf) into 62 doubles, in the record layout of
+ * oracle/ref_pin/pin_decoders.cpp, which decodes with the reference's own
+ * vulkan_acceleration_structure_util.h.  Returns 0 or -1. */
+int oracle_decode_node(const uint8_t* blob, uint32_t unit, int kind, double* out);
+
 /* createTreelets + buildNodeToRootMap over a blob (vulkan_ray_tracing.cc:823-1470,
  * :475-489).  Returns NULL on a condition where the reference asserts; the
  * message is in oracle_last_error(). */

@@ -95,12 +95,23 @@ def build_oracle(verbose: bool = False, force: bool = False) -> str:
     return ORACLE_LIB
 
 
+def build_reference_pin(verbose: bool = False) -> None:
+    """Builds oracle/_ref/pin_decoders from the reference's own decoder header
+    when the reference tree is present (it is not on every machine)."""
+    ref = os.environ.get("TREELET_RT_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src", "cuda-sim")):
+        return
+    _run(["make", "-s", "-C", os.path.join(ORACLE_DIR, "ref_pin"), f"REFERENCE={ref}"], verbose)
+
+
 def build_all(verbose: bool = False, force: bool = False) -> None:
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    with ThreadPoolExecutor(max_workers=3) as ex:
         a = ex.submit(build_library, verbose, force)
         b = ex.submit(build_oracle, verbose, force)
+        c = ex.submit(build_reference_pin, verbose)
         a.result()
         b.result()
+        c.result()
 
 
 if __name__ == "__main__":
