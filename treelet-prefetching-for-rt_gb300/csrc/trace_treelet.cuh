@@ -11,8 +11,9 @@ constexpr uint32_t kSlotBitsDev = 10;
 // (push_front / pop_front on std::list, :1708-1709): `cur` holds nodes of the
 // current treelet, `oth` the rest (:1821-1856).  An entry packs the node
 // (unit << 2 | top | leaf) and, for bottom-level nodes, the instance leaf it
-// belongs to; with STAGED it also keeps the node's staged location
-// (dense treelet << 10 | 64-byte slot in that treelet's image).
+// belongs to.  The staged location of a node (dense treelet << 10 | 64-byte
+// slot in that treelet's image) is read from the node table when needed, not
+// kept on the stacks.
 template <int CAP, bool STAGED>
 struct Walker {
   rtm::V3 O, D, idir;
@@ -21,7 +22,6 @@ struct Walker {
   uint32_t c_leaf, c_inst, current_root, status;
   int cn, on;
   unsigned long long cu[CAP], ot[CAP];
-  uint32_t cu_loc[STAGED ? CAP : 1], ot_loc[STAGED ? CAP : 1];
   InstCtx ic;
   Recorder rec;
   SceneView v;
@@ -29,44 +29,28 @@ struct Walker {
 
   __device__ __forceinline__ bool active() const { return cn > 0 || on > 0; }
 
-  // Staged location of the node the ray visits next (its first pending access).
+  // Staged location (dense treelet << 10 | slot) of the node the ray visits
+  // next, i.e. its first pending access.
   __device__ __forceinline__ uint32_t next_loc() const {
-    if (!STAGED) return kNone;
-    if (cn > 0) return cu_loc[cn - 1];
-    if (on > 0) return ot_loc[on - 1];
-    return kNone;
+    unsigned long long e;
+    if (cn > 0) e = cu[cn - 1];
+    else if (on > 0) e = ot[on - 1];
+    else return kNone;
+    const uint32_t unit = (uint32_t)e >> 2;
+    return unit < v.n_units ? __ldg(reinterpret_cast<const uint32_t*>(v.meta) + 2ull * unit + 1) : kNone;
   }
 
   // addrToTreeletID(child) == current_treelet_root ? current : other.
   __device__ __forceinline__ void route(const TraceArgs& a, uint32_t code, uint32_t inst) {
     const uint32_t unit = code >> 2;
-    uint32_t root = kNone, loc = kNone;
-    if (unit < v.n_units) {
-      if (STAGED) {
-        const uint2 m = __ldg(v.meta + unit);
-        root = m.x;
-        loc = m.y;
-      } else {
-        root = __ldg(reinterpret_cast<const uint32_t*>(v.meta) + 2ull * unit);
-      }
-    }
+    const uint32_t root = unit < v.n_units ? __ldg(reinterpret_cast<const uint32_t*>(v.meta) + 2ull * unit) : kNone;
     const unsigned long long e = (unsigned long long)code | ((unsigned long long)inst << 32);
     if (root == current_root) {
-      if (cn < CAP) {
-        cu[cn] = e;
-        if (STAGED) cu_loc[cn] = loc;
-        ++cn;
-      } else {
-        status |= RT_RAY_STACK_OVERFLOW;
-      }
+      if (cn < CAP) cu[cn++] = e;
+      else status |= RT_RAY_STACK_OVERFLOW;
     } else {
-      if (on < CAP) {
-        ot[on] = e;
-        if (STAGED) ot_loc[on] = loc;
-        ++on;
-      } else {
-        status |= RT_RAY_STACK_OVERFLOW;
-      }
+      if (on < CAP) ot[on++] = e;
+      else status |= RT_RAY_STACK_OVERFLOW;
     }
   }
 
@@ -105,21 +89,18 @@ struct Walker {
     ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
   }
 
-  // Visits one node; `lookup(loc)` returns its shared-memory address when it
-  // is staged, else 0.
+  // Visits one node; `lookup(unit, meta)` returns its shared-memory address
+  // when it is staged, else 0.
   template <class Lookup>
   __device__ __forceinline__ void step(const TraceArgs& a, Lookup&& lookup) {
     unsigned long long e;
-    uint32_t loc = kNone;
     if (cn == 0) {  // :1748-1754
       --on;
       e = ot[on];
-      if (STAGED) loc = ot_loc[on];
       current_root = (uint32_t)e >> 2;
     } else {
       --cn;
       e = cu[cn];
-      if (STAGED) loc = cu_loc[cn];
     }
     const uint32_t code = (uint32_t)e, inst = (uint32_t)(e >> 32);
     const uint32_t unit = code >> 2;
@@ -131,7 +112,7 @@ struct Walker {
     }
     uint32_t saddr = 0;
     if (STAGED) {
-      saddr = lookup(loc);
+      saddr = lookup(unit, v.meta);
       if (saddr) ++smem_reads;
       else ++gmem_reads;
     }
@@ -208,7 +189,7 @@ struct Walker {
   }
 
   __device__ __forceinline__ void step(const TraceArgs& a) {
-    step(a, [](uint32_t) -> uint32_t { return 0u; });
+    step(a, [](uint32_t, const uint2*) -> uint32_t { return 0u; });
   }
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
@@ -319,7 +300,12 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
     st.disabled = 0;
   }
   __syncwarp();
-  auto lookup = [&](uint32_t loc) -> uint32_t {
+  // the node's location is read only while some slot of the warp is resident
+  auto lookup = [&](uint32_t unit, const uint2* meta) -> uint32_t {
+    bool any = false;
+    for (uint32_t s = 0; s < slots; ++s) any |= st.resident[s] != kNone;
+    if (!any) return 0u;
+    const uint32_t loc = __ldg(reinterpret_cast<const uint32_t*>(meta) + 2ull * unit + 1);
     if (loc == kNone) return 0u;
     const uint32_t d = loc >> kSlotBitsDev, u = loc & ((1u << kSlotBitsDev) - 1u);
     for (uint32_t s = 0; s < slots; ++s)
