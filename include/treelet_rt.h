@@ -218,6 +218,18 @@ rt_status rt_partition_get(const rt_partition* p, uint32_t* roots, uint64_t* mem
                            uint16_t* member_bytes, uint32_t* node_root);
 rt_status rt_partition_remap(const rt_partition* p, uint32_t stride, uint64_t* new_addr);
 void rt_partition_free(rt_partition* p);
+/* Routing bits of the treelet-ordered walk per unit (n_units entries; no
+ * reference counterpart, they restate the addrToTreeletID comparisons of
+ * traceRayWithTreelets, vulkan_ray_tracing.cc:1821-1856, per node): bit i:
+ * internal child i shares the node's treelet root; bit 6 + i: child i's
+ * treelet root is the node; bits 12 / 13: the same for an instance leaf's
+ * BLAS root.  `blob` must be the one the partition was formed on. */
+rt_status rt_partition_route(const rt_partition* p, const rt_blob* blob, uint16_t* route);
+/* The pinned image for `order` (NULL: default order) and `budget` bytes:
+ * out == NULL only reports its size in *n_bytes; else out receives *n_bytes
+ * bytes.  *root_soff: record of the TLAS root in 16-byte units, 0 if absent. */
+rt_status rt_partition_pinned(const rt_partition* p, const rt_blob* blob, const uint32_t* order, uint32_t n_order,
+                              uint32_t budget, void* out, uint64_t* n_bytes, uint32_t* root_soff);
 
 /* Treelet-contiguous relayout (remapBVHToTreeletLayout,
  * vulkan_ray_tracing.cc:1473-1509): new_addr[u] for every unit, or
@@ -264,20 +276,41 @@ rt_status rt_trace_host_noalloc(rt_scene* scene, const rt_ray* rays, const uint3
  * changes a result. */
 rt_status rt_scene_set_stage_hints(rt_scene* scene, const uint32_t* hints);
 
-/* Traversal tuning; 0 keeps the current value.  None of these changes any
- * result, only speed. */
+/* Traversal tuning; 0 keeps the current value, RT_TUNING_OFF switches a
+ * feature off where noted.  None of these changes any result, only speed. */
+#define RT_TUNING_OFF 0xFFFFFFFFu
 typedef struct rt_tuning {
   uint32_t block_threads;     /* threads per CTA for RT_MODE_PLAIN / RT_MODE_TREELET (32..256) */
-  uint32_t staged_threads;    /* threads per CTA for RT_MODE_STAGED (32..256) */
+  uint32_t staged_threads;    /* threads per CTA for RT_MODE_STAGED (32..512) */
   uint32_t staged_epoch;      /* node visits of a warp between staging votes */
-  uint32_t staged_slots;      /* shared-memory treelet slots per warp (1..8) */
+  uint32_t staged_slots;      /* shared-memory treelet slots per warp (1..8; RT_TUNING_OFF: none) */
   uint32_t refill_lanes;      /* idle lanes of a warp that make it fetch new rays (1..32) */
   uint32_t staged_slot_bytes; /* bytes per slot: a treelet's first bytes when smaller than it */
   uint32_t staged_min_votes;  /* lanes of a warp that must want a treelet to stage it (1..32) */
   uint32_t stack_depth;       /* traversal stack entries per ray: 48, 96 or 160 (deeper rays are flagged) */
+  uint32_t pinned_bytes;      /* shared memory per CTA for pinned treelets (256..229376; RT_TUNING_OFF: none) */
 } rt_tuning;
 rt_status rt_scene_set_tuning(rt_scene* scene, const rt_tuning* t);
 rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);
+
+/* Pinned treelets (RT_MODE_STAGED; no reference counterpart).  Each CTA of a
+ * staged launch copies the pinned image into shared memory once, with
+ * cp.async.bulk, and serves every read of a pinned node from it for the
+ * whole launch.  The image holds the pinned treelets' nodes already decoded
+ * (internal nodes as FP32 child bounds computed with the walk's own
+ * operations), so results are unchanged.  Treelets are pinned in `order`
+ * (dense ids, most wanted first) while they fit in tuning.pinned_bytes;
+ * order == NULL restores the default order: the TLAS treelet, then treelets
+ * by the surface-area probability of their root. */
+rt_status rt_scene_set_pin_order(rt_scene* scene, const uint32_t* order, uint32_t n);
+typedef struct rt_pinned_info {
+  uint32_t bytes;       /* image size (0: nothing pinned) */
+  uint32_t n_treelets;  /* treelets pinned */
+  uint32_t n_records;   /* nodes pinned */
+  uint32_t root_pinned; /* 1 if the TLAS root node is pinned */
+} rt_pinned_info;
+/* The image the next staged launch uses, built now if needed. */
+rt_status rt_scene_pinned_info(rt_scene* scene, rt_pinned_info* info);
 
 /* Counters of the last rt_trace on this scene (read after the stream is
  * synchronised): node bytes read by the walk, bytes copied into shared memory

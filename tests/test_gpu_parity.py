@@ -132,6 +132,59 @@ def test_staged_tuning_invariance(ctx, tuning):
     _check_all_modes(ctx, blob, rays, tuning=tuning)
 
 
+OFF = 0xFFFFFFFF
+
+
+@pytest.mark.parametrize("tuning", [dict(pinned_bytes=OFF),
+                                    dict(pinned_bytes=1024, staged_slots=OFF),
+                                    dict(pinned_bytes=16384, staged_epoch=1, staged_min_votes=1),
+                                    dict(pinned_bytes=200000, staged_slots=OFF, staged_threads=512),
+                                    dict(pinned_bytes=65536, staged_threads=256, staged_slots=2, refill_lanes=1)])
+@pytest.mark.parametrize("scene_kind", ["terrain", "shared_blas", "bounce"])
+def test_pinned_treelets_invariance(ctx, tuning, scene_kind):
+    """Pinned (decoded, shared-memory) treelets change where node bytes come
+    from, never a hit, a visit or a treelet id."""
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    if scene_kind == "terrain":
+        blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 64 * 64, 5)
+        rays = rt.camera_rays(rt.default_camera(rt.SCENE_TERRAIN_INSTANCES), 48, 48, 1, 3, 1e-4, 1e30)
+    elif scene_kind == "shared_blas":
+        blob = rt.Blob.gen(rt.SCENE_SHARED_BLAS, 512, 4)
+        rays = rt.camera_rays(rt.default_camera(rt.SCENE_SHARED_BLAS), 48, 48, 1, 9, 1e-4, 1e30)
+    else:
+        blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 16384, 2)
+        prim = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 64, 64, 1, 5, 1e-4, 1e30)
+        ph, _, _ = orc.trace(blob.bytes(), prim, 0)
+        rays = rt.bounce_rays_host(blob, prim, ph, seed=11)
+    _check_all_modes(ctx, blob, rays, tuning=tuning)
+
+
+def test_pinned_treelets_serve_reads(ctx):
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 64 * 64, 5)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_TERRAIN_INSTANCES), 64, 64, 1, 3, 1e-4, 1e30)
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    scene.set_tuning(pinned_bytes=131072, staged_slots=OFF)
+    info = scene.pinned_info()
+    assert info["root_pinned"] == 1 and 0 < info["bytes"] <= 131072 and info["n_records"] > 0
+    ref, _, _ = scene.trace_host(rays, rt.MODE_TREELET)
+    hits, _, _ = scene.trace_host(rays, rt.MODE_STAGED)
+    assert_hits_equal(hits, ref, "pinned staged vs treelet order")
+    st = scene.stats()
+    assert st["device_status"] == 0
+    assert st["smem_reads"] > 0 and st["staged_bytes"] > 0
+    # a custom order naming no reachable treelet pins nothing
+    scene.set_pin_order([scene.treelet_info["n_treelets"] - 1])
+    assert scene.pinned_info()["bytes"] == 0
+    scene.set_pin_order(None)
+    assert scene.pinned_info()["root_pinned"] == 1
+    scene.close()
+
+
 def test_empty_batch(ctx):
     import treelet_rt as rt
 

@@ -108,11 +108,19 @@ struct rt_scene {
   uint16_t* d_member_bytes = nullptr;
   uint32_t* d_hint = nullptr;  // staged-mode predictions (8 per treelet) or null
   uint32_t slot_bytes = 0;
+  std::vector<uint16_t> route;  // routing bits of the treelet-ordered walk
+  uint16_t* d_route = nullptr;
+  // pinned treelets of the staged walk (built when treelets, order or budget change)
+  std::vector<uint32_t> pin_order;  // explicit order, empty = default
+  std::vector<uint32_t> pin_default;
+  uint8_t* d_pin = nullptr;
+  rt_pinned_info pin_info{0, 0, 0, 0};
+  uint32_t pin_root = 0;
   // per-launch counters and status (library scratch)
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
-  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96};
+  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, 98304};
   // host-buffer path scratch
   cudaStream_t stream = nullptr;
   void* d_io = nullptr;
@@ -151,6 +159,15 @@ void free_treelets(rt_scene* s) {
   cudaFree(s->d_member_first);
   cudaFree(s->d_member_bytes);
   cudaFree(s->d_hint);
+  cudaFree(s->d_route);
+  cudaFree(s->d_pin);
+  s->d_route = nullptr;
+  s->d_pin = nullptr;
+  s->pin_info = rt_pinned_info{0, 0, 0, 0};
+  s->pin_root = 0;
+  s->route.clear();
+  s->pin_default.clear();
+  s->pin_order.clear();
   s->d_hint = nullptr;
   s->d_meta = nullptr;
   s->d_images = nullptr;
@@ -204,6 +221,82 @@ int max_smem_per_block() {
   return v;
 }
 
+// Dynamic shared memory a staged CTA can use next to its static state.
+uint32_t staged_smem_limit() {
+  const int v = max_smem_per_block() - (int)(sizeof(rtk::WarpStage) * (rtk::kStagedMaxThreads / 32)) - 1024;
+  return v > 0 ? (uint32_t)v : 0u;
+}
+
+// Rebuilds the pinned image for the scene's order and budget (the budget is
+// clamped to what a CTA can hold).
+rt_status rebuild_pinned(rt_scene* s) {
+  cudaFree(s->d_pin);
+  s->d_pin = nullptr;
+  s->pin_info = rt_pinned_info{0, 0, 0, 0};
+  s->pin_root = 0;
+  const uint32_t want = s->tuning.pinned_bytes;
+  if (!s->has_treelets || want == RT_TUNING_OFF || want == 0) return RT_OK;
+  const uint32_t budget = std::min(want, staged_smem_limit() > 128 ? staged_smem_limit() - 128 : 0u);
+  if (s->pin_default.empty() && s->pin_order.empty())
+    rtt::default_pin_order(s->host_blob.data(), s->blob_bytes, s->pin_default, s->part);
+  rtt::Pinned pin;
+  rtt::build_pinned(s->host_blob.data(), s->blob_bytes, s->part, s->route,
+                    s->pin_order.empty() ? s->pin_default : s->pin_order, budget, pin);
+  if (pin.bytes.empty()) return RT_OK;
+  rt_status st = dalloc(&s->d_pin, pin.bytes.size());
+  if (st != RT_OK) return st;
+  RT_CUDA(cudaMemcpy(s->d_pin, pin.bytes.data(), pin.bytes.size(), cudaMemcpyHostToDevice));
+  s->pin_info = rt_pinned_info{(uint32_t)pin.bytes.size(), pin.n_treelets, pin.n_records, pin.root_soff ? 1u : 0u};
+  s->pin_root = pin.root_soff;
+  return RT_OK;
+}
+
+// Merges the nonzero fields of `t` into `cur` after checking them.
+rt_status merge_tuning(const rt_tuning& cur, const rt_tuning* t, rt_tuning& n) {
+  n = cur;
+  auto ok_threads = [](uint32_t v, uint32_t hi) { return v >= 32 && v <= hi && v % 32 == 0; };
+  if (t->block_threads) {
+    if (!ok_threads(t->block_threads, 256))
+      return rti::fail(RT_ERR_INVALID, "block_threads must be 32..256, multiple of 32");
+    n.block_threads = t->block_threads;
+  }
+  if (t->staged_threads) {
+    if (!ok_threads(t->staged_threads, rtk::kStagedMaxThreads))
+      return rti::fail(RT_ERR_INVALID, "staged_threads must be 32..512, multiple of 32");
+    n.staged_threads = t->staged_threads;
+  }
+  if (t->staged_epoch) n.staged_epoch = t->staged_epoch;
+  if (t->refill_lanes) {
+    if (t->refill_lanes > 32) return rti::fail(RT_ERR_INVALID, "refill_lanes must be 1..32");
+    n.refill_lanes = t->refill_lanes;
+  }
+  if (t->staged_slots) {
+    if (t->staged_slots != RT_TUNING_OFF && t->staged_slots > (uint32_t)rtk::kMaxSlots)
+      return rti::fail(RT_ERR_INVALID, "staged_slots must be 1..8 or RT_TUNING_OFF");
+    n.staged_slots = t->staged_slots;
+  }
+  if (t->staged_slot_bytes) {
+    if (t->staged_slot_bytes < 64 || t->staged_slot_bytes > 65536)
+      return rti::fail(RT_ERR_INVALID, "staged_slot_bytes must be 64..65536");
+    n.staged_slot_bytes = t->staged_slot_bytes;
+  }
+  if (t->staged_min_votes) {
+    if (t->staged_min_votes > 32) return rti::fail(RT_ERR_INVALID, "staged_min_votes must be 1..32");
+    n.staged_min_votes = t->staged_min_votes;
+  }
+  if (t->stack_depth) {
+    if (t->stack_depth != 48 && t->stack_depth != 96 && t->stack_depth != 160)
+      return rti::fail(RT_ERR_INVALID, "stack_depth must be 48, 96 or 160");
+    n.stack_depth = t->stack_depth;
+  }
+  if (t->pinned_bytes) {
+    if (t->pinned_bytes != RT_TUNING_OFF && (t->pinned_bytes < 256 || t->pinned_bytes > 229376))
+      return rti::fail(RT_ERR_INVALID, "pinned_bytes must be 256..229376 or RT_TUNING_OFF");
+    n.pinned_bytes = t->pinned_bytes;
+  }
+  return RT_OK;
+}
+
 // Zeroes the launch's counters and queue, then launches the kernel of `mode`
 // with stack depth CAP.
 template <int CAP>
@@ -227,14 +320,19 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
     // per-warp slots: the whole largest image, or the first staged_slot_bytes of each
     uint32_t slot_bytes = largest_image;
     if (t.staged_slot_bytes) slot_bytes = std::min(slot_bytes, (t.staged_slot_bytes + 127u) & ~127u);
-    uint32_t slots = t.staged_slots;
-    const int limit = max_smem_per_block() - (int)(sizeof(rtk::WarpStage) * 8) - 1024;
-    while (slots > 0 && (int)(warps * slots * slot_bytes + 128) > limit) --slots;
+    uint32_t slots = t.staged_slots == RT_TUNING_OFF ? 0u : t.staged_slots;
+    if (slot_bytes == 0) slots = 0;
+    const uint64_t limit = staged_smem_limit();
+    if ((uint64_t)a.pin_bytes + 128 > limit) {  // cannot happen for images built by rebuild_pinned
+      a.pin_bytes = 0;
+      a.pin_root = 0;
+    }
+    while (slots > 0 && (uint64_t)a.pin_bytes + (uint64_t)warps * slots * slot_bytes + 128 > limit) --slots;
     a.slots = slots;
     a.slot_bytes = slot_bytes;
     a.min_votes = t.staged_min_votes;
-    const size_t dyn = (size_t)warps * slots * slot_bytes + 128;
-    auto kern = rtk::trace_staged_kernel<CAP>;
+    const size_t dyn = (size_t)a.pin_bytes + (size_t)warps * slots * slot_bytes + 128;
+    auto kern = slots ? rtk::trace_staged_kernel<CAP, true> : rtk::trace_staged_kernel<CAP, false>;
     RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     kern<<<persistent_grid((const void*)kern, bt, a.n, dyn), bt, dyn, st>>>(a);
   }
@@ -294,6 +392,8 @@ rt_status rt_scene_create(rt_ctx* ctx, const rt_blob* blob, rt_scene** out) {
   *out = nullptr;
   std::string err;
   if (!rti::validate_blob(blob->bytes.data(), blob->bytes.size(), &err)) return rti::fail(RT_ERR_BLOB, err);
+  if (blob->bytes.size() / 64 >= (1ull << 29))
+    return rti::fail(RT_ERR_TOO_LARGE, "rt_scene_create: blobs are limited to 2^29 units of 64 bytes");
   RT_CUDA(cudaSetDevice(ctx->device));
   auto* s = new rt_scene();
   s->ctx = ctx;
@@ -376,7 +476,19 @@ rt_status rt_treelets_form(rt_scene* s, uint32_t max_treelet_bytes, rt_treelet_i
                        cudaMemcpyHostToDevice));
   s->slot_bytes = (p.largest_image + 127u) & ~127u;
   s->part = std::move(p);
+  rtt::route_masks(s->host_blob.data(), s->blob_bytes, s->part, s->route);
+  st = dalloc(&s->d_route, sizeof(uint16_t) * s->route.size());
+  if (st != RT_OK) {
+    free_treelets(s);
+    return st;
+  }
+  RT_CUDA(cudaMemcpy(s->d_route, s->route.data(), sizeof(uint16_t) * s->route.size(), cudaMemcpyHostToDevice));
   s->has_treelets = true;
+  st = rebuild_pinned(s);
+  if (st != RT_OK) {
+    free_treelets(s);
+    return st;
+  }
   if (info) {
     info->n_treelets = n;
     info->max_treelet_bytes = max_treelet_bytes;
@@ -413,40 +525,31 @@ rt_status rt_treelets_remap(const rt_scene* s, uint32_t stride, uint64_t* new_ad
 
 rt_status rt_scene_set_tuning(rt_scene* s, const rt_tuning* t) {
   if (!s || !t) return rti::fail(RT_ERR_INVALID, "rt_scene_set_tuning: NULL");
-  rt_tuning n = s->tuning;
-  auto ok_threads = [](uint32_t v) { return v >= 32 && v <= 256 && v % 32 == 0; };
-  if (t->block_threads) {
-    if (!ok_threads(t->block_threads)) return rti::fail(RT_ERR_INVALID, "block_threads must be 32..256, multiple of 32");
-    n.block_threads = t->block_threads;
-  }
-  if (t->staged_threads) {
-    if (!ok_threads(t->staged_threads)) return rti::fail(RT_ERR_INVALID, "staged_threads must be 32..256, multiple of 32");
-    n.staged_threads = t->staged_threads;
-  }
-  if (t->staged_epoch) n.staged_epoch = t->staged_epoch;
-  if (t->refill_lanes) {
-    if (t->refill_lanes > 32) return rti::fail(RT_ERR_INVALID, "refill_lanes must be 1..32");
-    n.refill_lanes = t->refill_lanes;
-  }
-  if (t->staged_slots) {
-    if (t->staged_slots > (uint32_t)rtk::kMaxSlots) return rti::fail(RT_ERR_INVALID, "staged_slots must be 1..8");
-    n.staged_slots = t->staged_slots;
-  }
-  if (t->staged_slot_bytes) {
-    if (t->staged_slot_bytes < 64 || t->staged_slot_bytes > 65536)
-      return rti::fail(RT_ERR_INVALID, "staged_slot_bytes must be 64..65536");
-    n.staged_slot_bytes = t->staged_slot_bytes;
-  }
-  if (t->staged_min_votes) {
-    if (t->staged_min_votes > 32) return rti::fail(RT_ERR_INVALID, "staged_min_votes must be 1..32");
-    n.staged_min_votes = t->staged_min_votes;
-  }
-  if (t->stack_depth) {
-    if (t->stack_depth != 48 && t->stack_depth != 96 && t->stack_depth != 160)
-      return rti::fail(RT_ERR_INVALID, "stack_depth must be 48, 96 or 160");
-    n.stack_depth = t->stack_depth;
-  }
+  rt_tuning n;
+  rt_status st = merge_tuning(s->tuning, t, n);
+  if (st != RT_OK) return st;
+  const bool repin = n.pinned_bytes != s->tuning.pinned_bytes;
   s->tuning = n;
+  if (repin && s->has_treelets) {
+    RT_CUDA(cudaSetDevice(s->ctx->device));
+    return rebuild_pinned(s);
+  }
+  return RT_OK;
+}
+
+rt_status rt_scene_set_pin_order(rt_scene* s, const uint32_t* order, uint32_t n) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_scene_set_pin_order: NULL scene");
+  if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_scene_set_pin_order: call rt_treelets_form first");
+  if (order && n == 0) return rti::fail(RT_ERR_INVALID, "rt_scene_set_pin_order: empty order");
+  if (order) s->pin_order.assign(order, order + n);
+  else s->pin_order.clear();
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  return rebuild_pinned(s);
+}
+
+rt_status rt_scene_pinned_info(rt_scene* s, rt_pinned_info* info) {
+  if (!s || !info) return rti::fail(RT_ERR_INVALID, "rt_scene_pinned_info: NULL");
+  *info = s->pin_info;
   return RT_OK;
 }
 
@@ -483,6 +586,12 @@ rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint3
   a.tl_trace = trace ? trace->treelets : nullptr;
   a.cap = (trace && (trace->visits || trace->treelets)) ? trace->capacity : 0;
   a.meta = s->d_meta;
+  a.route = s->d_route;
+  if (mode == RT_MODE_STAGED && s->d_pin) {
+    a.pin_image = reinterpret_cast<const uint4*>(s->d_pin);
+    a.pin_bytes = s->pin_info.bytes;
+    a.pin_root = s->pin_root;
+  }
   a.images = reinterpret_cast<const uint4*>(s->d_images);
   a.image_off = s->d_image_off;
   a.n_treelets = s->has_treelets ? (uint32_t)s->part.roots.size() : 0;
@@ -638,13 +747,14 @@ struct rt_batch {
   rt_ctx* ctx = nullptr;
   std::vector<rt_scene*> scenes;
   rtk::SceneView* d_views = nullptr;
+  std::vector<rtk::SceneView> views;  // host copy of d_views
   uint32_t* d_item_begin = nullptr;
   uint32_t* d_item_scene = nullptr;
   uint32_t n_items = 0, n_rays = 0;
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;
-  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96};
+  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, RT_TUNING_OFF};  // batches pin nothing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -667,6 +777,21 @@ rt_status batch_args(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uin
   if (mode == RT_MODE_TREELET)
     for (rt_scene* s : b->scenes)
       if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_trace_batch: a scene has no treelets");
+  // scenes may have (re)formed their treelets since the views were uploaded
+  bool stale = false;
+  for (size_t i = 0; i < b->scenes.size(); ++i) {
+    const rt_scene* s = b->scenes[i];
+    const rtk::SceneView nv{reinterpret_cast<const uint4*>(s->d_blob), s->d_meta, s->d_route, s->n_units};
+    const rtk::SceneView& ov = b->views[i];
+    if (nv.blob != ov.blob || nv.meta != ov.meta || nv.route != ov.route || nv.n_units != ov.n_units) {
+      b->views[i] = nv;
+      stale = true;
+    }
+  }
+  if (stale) {
+    RT_CUDA(cudaSetDevice(b->ctx->device));
+    RT_CUDA(cudaMemcpy(b->d_views, b->views.data(), sizeof(rtk::SceneView) * b->views.size(), cudaMemcpyHostToDevice));
+  }
   a = rtk::TraceArgs{};
   a.scenes = b->d_views;
   a.item_begin = b->d_item_begin;
@@ -708,9 +833,11 @@ rt_status rt_batch_create(rt_ctx* ctx, rt_scene* const* scenes, uint32_t n_scene
       rt_batch_destroy(b);
       return rti::fail(RT_ERR_INVALID, "rt_batch_create: NULL scene or scene on another device");
     }
-    v[i] = rtk::SceneView{reinterpret_cast<const uint4*>(scenes[i]->d_blob), scenes[i]->d_meta, scenes[i]->n_units};
+    v[i] = rtk::SceneView{reinterpret_cast<const uint4*>(scenes[i]->d_blob), scenes[i]->d_meta, scenes[i]->d_route,
+                          scenes[i]->n_units};
   }
   cudaError_t e = cudaMemcpy(b->d_views, v.data(), sizeof(rtk::SceneView) * n_scenes, cudaMemcpyHostToDevice);
+  b->views = v;
   if (e != cudaSuccess) {
     rt_batch_destroy(b);
     return cuda_fail(e, "rt_batch_create");
@@ -757,12 +884,10 @@ rt_status rt_batch_set_items(rt_batch* b, const uint32_t* ray_begin, const uint3
 
 rt_status rt_batch_set_tuning(rt_batch* b, const rt_tuning* t) {
   if (!b || !t || b->scenes.empty()) return rti::fail(RT_ERR_INVALID, "rt_batch_set_tuning: NULL");
-  // validate through a scene's setter, then keep a copy for the batch
-  rt_tuning keep = b->scenes[0]->tuning;
-  rt_status st = rt_scene_set_tuning(b->scenes[0], t);
+  rt_tuning n;
+  rt_status st = merge_tuning(b->tuning, t, n);
   if (st != RT_OK) return st;
-  b->tuning = b->scenes[0]->tuning;
-  b->scenes[0]->tuning = keep;
+  b->tuning = n;
   return RT_OK;
 }
 

@@ -23,6 +23,12 @@ __device__ __forceinline__ uint4 ld_shared_v4(uint32_t saddr) {
   return v;
 }
 
+__device__ __forceinline__ uint32_t ld_shared_u32(uint32_t saddr) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(saddr));
+  return v;
+}
+
 // Loads 64 bytes: from shared memory when saddr != 0, else from global.
 __device__ __forceinline__ void load64(const uint4* g, uint32_t saddr, Node64& n) {
 #pragma unroll
@@ -73,6 +79,22 @@ __device__ __forceinline__ float mx2(float a, float b) {
   return rtm::tmax2(a, b);
 }
 
+// One child's slab test from its six plane distances, reduced as magic_max7 /
+// magic_min7 (vulkan_ray_tracing.cc:199-218); a hit at thit >= cull is dropped.
+template <bool FAST>
+__device__ __forceinline__ bool slab_hit(float lx, float ly, float lz, float hx, float hy, float hz, float tmin,
+                                         float tmax, float cull) {
+  const float t1 = mx2<FAST>(mn2<FAST>(lx, hx), tmin);
+  const float t2 = mx2<FAST>(mn2<FAST>(ly, hy), t1);
+  const float tn = mx2<FAST>(mn2<FAST>(lz, hz), t2);
+  const float u1 = mn2<FAST>(mx2<FAST>(lx, hx), tmax);
+  const float u2 = mn2<FAST>(mx2<FAST>(ly, hy), u1);
+  const float tf = mn2<FAST>(mx2<FAST>(lz, hz), u2);
+  bool h = tn <= tf;
+  if (h && tn >= cull) h = false;
+  return h;
+}
+
 // The box tests of an internal node (vulkan_ray_tracing.cc:2518-2553 and the
 // bottom-level twin :2714-2741): children with ChildSize > 0 are slab-tested
 // with the ray's [tmin, tmax]; a hit at thit >= cull is dropped.  Bounds are
@@ -100,15 +122,7 @@ __device__ __forceinline__ ChildHits test_children(const Node64& n, uint32_t nod
       const float hx = ((ox + byte_as_float(n, rtf::IN_HI_X + i) * sx) - o.x) * idir.x;
       const float hy = ((oy + byte_as_float(n, rtf::IN_HI_Y + i) * sy) - o.y) * idir.y;
       const float hz = ((oz + byte_as_float(n, rtf::IN_HI_Z + i) * sz) - o.z) * idir.z;
-      const float t1 = mx2<FAST>(mn2<FAST>(lx, hx), tmin);
-      const float t2 = mx2<FAST>(mn2<FAST>(ly, hy), t1);
-      const float tn = mx2<FAST>(mn2<FAST>(lz, hz), t2);
-      const float u1 = mn2<FAST>(mx2<FAST>(lx, hx), tmax);
-      const float u2 = mn2<FAST>(mx2<FAST>(ly, hy), u1);
-      const float tf = mn2<FAST>(mx2<FAST>(lz, hz), u2);
-      bool h = tn <= tf;
-      if (h && tn >= cull) h = false;
-      if (h) r.hit_mask |= 1u << i;
+      if (slab_hit<FAST>(lx, ly, lz, hx, hy, hz, tmin, tmax, cull)) r.hit_mask |= 1u << i;
     }
   }
   return r;

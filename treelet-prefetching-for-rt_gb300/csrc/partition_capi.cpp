@@ -59,4 +59,34 @@ rt_status rt_partition_remap(const rt_partition* r, uint32_t stride, uint64_t* n
 
 void rt_partition_free(rt_partition* r) { delete r; }
 
+rt_status rt_partition_route(const rt_partition* r, const rt_blob* blob, uint16_t* route) {
+  if (!r || !blob || !route) return rti::fail(RT_ERR_INVALID, "rt_partition_route: NULL");
+  if (blob->bytes.size() / 64 != r->n_units) return rti::fail(RT_ERR_INVALID, "rt_partition_route: blob size differs");
+  std::vector<uint16_t> m;
+  rtt::route_masks(blob->bytes.data(), blob->bytes.size(), r->p, m);
+  std::copy(m.begin(), m.end(), route);
+  return RT_OK;
+}
+
+rt_status rt_partition_pinned(const rt_partition* r, const rt_blob* blob, const uint32_t* order, uint32_t n_order,
+                              uint32_t budget, void* out, uint64_t* n_bytes, uint32_t* root_soff) {
+  if (!r || !blob || !n_bytes) return rti::fail(RT_ERR_INVALID, "rt_partition_pinned: NULL");
+  if (blob->bytes.size() / 64 != r->n_units) return rti::fail(RT_ERR_INVALID, "rt_partition_pinned: blob size differs");
+  const uint8_t* b = blob->bytes.data();
+  std::vector<uint16_t> route;
+  rtt::route_masks(b, blob->bytes.size(), r->p, route);
+  std::vector<uint32_t> ord;
+  if (order) ord.assign(order, order + n_order);
+  else rtt::default_pin_order(b, blob->bytes.size(), ord, r->p);
+  rtt::Pinned pin;
+  rtt::build_pinned(b, blob->bytes.size(), r->p, route, ord, budget, pin);
+  if (out) {
+    if (*n_bytes < pin.bytes.size()) return rti::fail(RT_ERR_INVALID, "rt_partition_pinned: output too small");
+    std::copy(pin.bytes.begin(), pin.bytes.end(), static_cast<uint8_t*>(out));
+  }
+  *n_bytes = pin.bytes.size();
+  if (root_soff) *root_soff = pin.root_soff;
+  return RT_OK;
+}
+
 }  // extern "C"

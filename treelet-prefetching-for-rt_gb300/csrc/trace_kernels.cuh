@@ -36,7 +36,8 @@ constexpr uint32_t kStatusTimeout = 1u;
 // What a walk needs of one scene.
 struct SceneView {
   const uint4* blob;
-  const uint2* meta;  // per unit: x = treelet root unit, y = dense << 10 | slot
+  const uint2* meta;      // per unit: x = treelet root unit, y = dense << 10 | slot
+  const uint16_t* route;  // per unit: routing bits of the treelet-ordered walk (treelets.h)
   uint32_t n_units;
 };
 
@@ -58,6 +59,10 @@ struct TraceArgs {
   uint32_t* tl_trace;
   uint32_t cap;
   const uint2* meta;           // per unit: x = treelet root unit, y = dense << 10 | slot
+  const uint16_t* route;       // per unit: routing bits of the treelet-ordered walk
+  const uint4* pin_image;      // staged: pinned-treelet records (pinned.h), copied to shared memory per CTA
+  uint32_t pin_bytes;          // its size (multiple of 128), 0 = nothing pinned
+  uint32_t pin_root;           // record of the TLAS root node, 0 = not pinned
   const uint4* images;         // staged image store
   const unsigned long long* image_off;  // per dense treelet, n_treelets + 1
   uint32_t n_treelets;
@@ -101,7 +106,7 @@ __device__ __forceinline__ void load_ray(const rt_ray* rays, uint32_t r, rtm::V3
 
 // The scene ray r walks.
 __device__ __forceinline__ SceneView scene_of(const TraceArgs& a, uint32_t r) {
-  if (a.n_items == 0) return SceneView{a.blob, a.meta, a.n_units};
+  if (a.n_items == 0) return SceneView{a.blob, a.meta, a.route, a.n_units};
   uint32_t lo = 0, hi = a.n_items;  // last item with item_begin <= r
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
@@ -112,6 +117,7 @@ __device__ __forceinline__ SceneView scene_of(const TraceArgs& a, uint32_t r) {
   SceneView v;
   v.blob = reinterpret_cast<const uint4*>(__ldg(reinterpret_cast<const unsigned long long*>(&s->blob)));
   v.meta = reinterpret_cast<const uint2*>(__ldg(reinterpret_cast<const unsigned long long*>(&s->meta)));
+  v.route = reinterpret_cast<const uint16_t*>(__ldg(reinterpret_cast<const unsigned long long*>(&s->route)));
   v.n_units = __ldg(&s->n_units);
   return v;
 }
@@ -257,7 +263,8 @@ struct PlainWalker {
   bool opaque, terminate, inblas, fast;
   uint32_t next, c_leaf, c_inst, status;
   int sp;
-  uint32_t stk[CAP];
+  uint32_t top;       // stack entry sp - 1, kept in a register
+  uint32_t stk[CAP];  // entries 0 .. sp - 2
   InstCtx ic;
   bool ic_fast;
   Recorder rec;
@@ -266,8 +273,21 @@ struct PlainWalker {
   __device__ __forceinline__ bool active() const { return next != kNone || sp > 0; }
 
   __device__ __forceinline__ void push(uint32_t e) {
-    if (sp < CAP) stk[sp++] = e;
-    else status |= RT_RAY_STACK_OVERFLOW;
+    if (sp < CAP) {
+      if (sp > 0) stk[sp - 1] = top;
+      top = e;
+      ++sp;
+    } else {
+      status |= RT_RAY_STACK_OVERFLOW;
+    }
+  }
+
+  // The refill of `top` is not needed until the next pop, so its load is off
+  // the path of the node visit that follows.
+  __device__ __forceinline__ uint32_t pop() {
+    const uint32_t e = top;
+    if (--sp > 0) top = stk[sp - 1];
+    return e;
   }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
@@ -384,8 +404,8 @@ struct PlainWalker {
     for (;;) {
       if (next != kNone) return visit_internal(a, next);
       if (inblas) {
-        if (sp > 0 && !(stk[sp - 1] & kTop)) {
-          const uint32_t e = stk[--sp];
+        if (sp > 0 && !(top & kTop)) {
+          const uint32_t e = pop();
           if (e & kLeaf) return visit_leaf(a, e >> 2);
           next = e >> 2;
           continue;
@@ -394,7 +414,7 @@ struct PlainWalker {
         continue;
       }
       if (sp == 0) return;
-      const uint32_t e = stk[--sp];
+      const uint32_t e = pop();
       if (!(e & kLeaf)) {
         next = e >> 2;
         continue;

@@ -1,57 +1,86 @@
 // Treelet-ordered traversal (traceRayWithTreelets, vulkan_ray_tracing.cc:1522-2307)
 // and its shared-memory staged variant.
 #pragma once
+#include "pinned.h"
 #include "trace_kernels.cuh"
 
 namespace rtk {
 
 constexpr uint32_t kSlotBitsDev = 10;
+// Stack entry of the treelet-ordered walk, low word:
+//   unit << 3 | top | leaf          node in global memory
+//   soff << 3 | kEPin | top | leaf  node held as a pinned record in shared memory
+// high word: the instance leaf a bottom-level node belongs to.
+constexpr uint32_t kEShift = 3, kEPin = 4;
+constexpr uint32_t kRouteOther = 6, kRouteInst = 12;  // route bits (treelets.h)
+
+// A LIFO stack whose top entry lives in a register: a pop takes the register
+// and reloads it from local memory, and that load is not needed until the
+// next pop, so it stays off the path of the node visit in between.
+template <int CAP>
+struct EStack {
+  unsigned long long top;
+  unsigned long long below[CAP];  // entries 0 .. n - 2
+  int n;
+  __device__ __forceinline__ bool push(unsigned long long e) {
+    if (n >= CAP) return false;
+    if (n > 0) below[n - 1] = top;
+    top = e;
+    ++n;
+    return true;
+  }
+  __device__ __forceinline__ unsigned long long pop() {
+    const unsigned long long e = top;
+    if (--n > 0) top = below[n - 1];
+    return e;
+  }
+};
 
 // A ray's treelet-ordered walk.  Two LIFO stacks as in the reference
-// (push_front / pop_front on std::list, :1708-1709): `cur` holds nodes of the
-// current treelet, `oth` the rest (:1821-1856).  An entry packs the node
-// (unit << 2 | top | leaf) and, for bottom-level nodes, the instance leaf it
-// belongs to.  The staged location of a node (dense treelet << 10 | 64-byte
-// slot in that treelet's image) is read from the node table when needed, not
-// kept on the stacks.
+// (push_front / pop_front on std::list, :1708-1709): `cu` holds nodes of the
+// current treelet, `ot` the rest (:1821-1856).  Which stack a child goes to
+// is read from the per-node route bits (treelets.h): a node popped from `cu`
+// is in the current treelet, and a node popped from `ot` becomes the current
+// treelet root, so the reference's addrToTreeletID comparison is fixed per
+// node and precomputed.  The staged location of a node (dense treelet << 10 |
+// 64-byte slot in that treelet's image) is read from the node table when a
+// warp has a staged slot; pinned nodes are named by their record.
 template <int CAP, bool STAGED>
 struct Walker {
   rtm::V3 O, D, idir;
   float tmin, tmax, min_thit, c_tobj;
   bool terminate, fast, ic_fast;  // FAST min/max allowed for the world / object ray
-  uint32_t c_leaf, c_inst, current_root, status;
-  int cn, on;
-  unsigned long long cu[CAP], ot[CAP];
+  uint32_t c_leaf, c_inst, status;
+  EStack<CAP> cu, ot;
   InstCtx ic;
   Recorder rec;
   SceneView v;
   uint32_t smem_reads, gmem_reads;
+  uint32_t pin_base;  // shared address of the pinned records, 0 = none
+  uint32_t pin_root;  // record of the TLAS root node, 0 = not pinned
 
-  __device__ __forceinline__ bool active() const { return cn > 0 || on > 0; }
+  __device__ __forceinline__ bool active() const { return cu.n > 0 || ot.n > 0; }
 
   // Staged location (dense treelet << 10 | slot) of the node the ray visits
-  // next, i.e. its first pending access.
+  // next, i.e. its first pending access; kNone for a pinned node.
   __device__ __forceinline__ uint32_t next_loc() const {
     unsigned long long e;
-    if (cn > 0) e = cu[cn - 1];
-    else if (on > 0) e = ot[on - 1];
+    if (cu.n > 0) e = cu.top;
+    else if (ot.n > 0) e = ot.top;
     else return kNone;
-    const uint32_t unit = (uint32_t)e >> 2;
+    if ((uint32_t)e & kEPin) return kNone;
+    const uint32_t unit = (uint32_t)e >> kEShift;
     return unit < v.n_units ? __ldg(reinterpret_cast<const uint32_t*>(v.meta) + 2ull * unit + 1) : kNone;
   }
 
-  // addrToTreeletID(child) == current_treelet_root ? current : other.
-  __device__ __forceinline__ void route(const TraceArgs& a, uint32_t code, uint32_t inst) {
-    const uint32_t unit = code >> 2;
-    const uint32_t root = unit < v.n_units ? __ldg(reinterpret_cast<const uint32_t*>(v.meta) + 2ull * unit) : kNone;
+  __device__ __forceinline__ void push(bool same, uint32_t code, uint32_t inst) {
     const unsigned long long e = (unsigned long long)code | ((unsigned long long)inst << 32);
-    if (root == current_root) {
-      if (cn < CAP) cu[cn++] = e;
-      else status |= RT_RAY_STACK_OVERFLOW;
-    } else {
-      if (on < CAP) ot[on++] = e;
-      else status |= RT_RAY_STACK_OVERFLOW;
-    }
+    if (!(same ? cu.push(e) : ot.push(e))) status |= RT_RAY_STACK_OVERFLOW;
+  }
+
+  __device__ __forceinline__ void bad_node() {
+    status |= RT_RAY_BAD_NODE;
+    cu.n = ot.n = 0;
   }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
@@ -62,11 +91,10 @@ struct Walker {
     rec = Recorder{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
                    a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, v.meta};
     status = 0;
-    cn = on = 0;
+    cu.n = ot.n = 0;
     min_thit = tmax;
     c_leaf = c_inst = 0;
     c_tobj = 0.0f;
-    current_root = 0;  // the TLAS header (:1707)
     ic.unit = kNone;
     smem_reads = gmem_reads = 0;
     idir = rtm::calculate_idir(D);
@@ -78,7 +106,13 @@ struct Walker {
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
     const rtm::V3 bmax = rtm::v3(__uint_as_float(h1.y), __uint_as_float(h1.z), __uint_as_float(h1.w));
     float th;
-    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) route(a, ((uint32_t)(root_off >> 6) << 2) | kTop, 0);
+    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) {
+      // current_treelet_root starts as the TLAS header, unit 0 (:1707)
+      const uint32_t code = ((uint32_t)(root_off >> 6) << kEShift) | kTop;
+      const uint32_t unit = code >> kEShift;
+      const uint32_t root = unit < v.n_units ? __ldg(&v.meta[unit].x) : kNone;
+      push(root == 0u, pin_root ? ((pin_root << kEShift) | kEPin | kTop) : code, 0);
+    }
   }
 
   __device__ __forceinline__ void ensure_instance(const TraceArgs& a, uint32_t inst) {
@@ -89,38 +123,44 @@ struct Walker {
     ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
   }
 
-  // Visits one node; `lookup(unit, meta)` returns its shared-memory address
-  // when it is staged, else 0.
+  // Visits one node; `lookup(unit, meta)` returns the shared-memory address
+  // of a node staged in a warp slot, else 0.
   template <class Lookup>
   __device__ __forceinline__ void step(const TraceArgs& a, Lookup&& lookup) {
-    unsigned long long e;
-    if (cn == 0) {  // :1748-1754
-      --on;
-      e = ot[on];
-      current_root = (uint32_t)e >> 2;
-    } else {
-      --cn;
-      e = cu[cn];
-    }
+    const bool from_cu = cu.n > 0;  // :1748-1754
+    const unsigned long long e = from_cu ? cu.pop() : ot.pop();
     const uint32_t code = (uint32_t)e, inst = (uint32_t)(e >> 32);
-    const uint32_t unit = code >> 2;
-    const bool top = code & kTop, leaf = code & kLeaf;
-    if (unit + ((top && leaf) ? 1u : 0u) >= v.n_units) {
-      status |= RT_RAY_BAD_NODE;
-      cn = on = 0;
-      return;
-    }
-    uint32_t saddr = 0;
-    if (STAGED) {
-      saddr = lookup(unit, v.meta);
-      if (saddr) ++smem_reads;
-      else ++gmem_reads;
+    const bool top = code & kTop, leaf = code & kLeaf, pinned = STAGED && (code & kEPin);
+    const uint32_t rsh = from_cu ? 0u : 1u;  // which route bit applies
+    uint32_t unit, rbits, saddr = 0;
+    if (pinned) {
+      saddr = pin_base + (code >> kEShift) * 16u;
+      unit = rtd::ld_shared_u32(saddr + (leaf ? 0u : rtp::IN_UNIT));
+      ++smem_reads;
+    } else {
+      unit = code >> kEShift;
+      if (unit + ((top && leaf) ? 1u : 0u) >= v.n_units) return bad_node();
+      if (STAGED) {
+        saddr = lookup(unit, v.meta);
+        if (saddr) ++smem_reads;
+        else ++gmem_reads;
+      }
     }
     const uint4* g = v.blob + (uint64_t)unit * 4;
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
       rec.rec(unit, rtf::TX_INTERNAL);
+      uint32_t soff01 = 0, soff23 = 0, soff45 = 0;
       rtd::Node64 nd;
       rtd::load64(g, saddr, nd);
+      if (pinned) {  // route bits in bytes 16..17, child records in the tail
+        const uint4 t = rtd::ld_shared_v4(saddr + rtp::IN_UNIT);
+        rbits = nd.w[rtp::IN_ROUTE / 4] & 0xffffu;
+        soff01 = t.y;
+        soff23 = t.z;
+        soff45 = t.w;
+      } else {
+        rbits = __ldg(v.route + unit);
+      }
       rtd::ChildHits ch;
       if (top) {
         ch = fast ? rtd::test_children<true>(nd, unit, O, idir, tmin, tmax, min_thit)
@@ -131,33 +171,59 @@ struct Walker {
         ch = ic_fast ? rtd::test_children<true>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull)
                      : rtd::test_children<false>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull);
       }
+      const uint32_t hit = ch.hit_mask;
+      const uint64_t info = ch.info;
+      const uint32_t same = rbits >> (rsh * kRouteOther);
       const uint32_t level = top ? kTop : 0u;
       uint32_t c = ch.child_unit;
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        const uint32_t info = ch.info_of(i);
-        if ((ch.hit_mask >> i) & 1u) {
-          const uint32_t lf = ((info >> 2) != rtf::CT_INTERNAL) ? kLeaf : 0u;
-          route(a, (c << 2) | level | lf, inst);
+        const uint32_t ci = (uint32_t)(info >> (8 * i)) & 0x3fu;
+        if ((hit >> i) & 1u) {
+          const uint32_t lf = ((ci >> 2) != rtf::CT_INTERNAL) ? kLeaf : 0u;
+          const uint32_t sw = i < 2 ? soff01 : (i < 4 ? soff23 : soff45);
+          const uint32_t so = (sw >> (16 * (i & 1))) & 0xffffu;
+          const uint32_t cc = so ? ((so << kEShift) | kEPin | level | lf) : ((c << kEShift) | level | lf);
+          push((same >> i) & 1u, cc, inst);
         }
-        c += info & 3u;
+        c += ci & 3u;
       }
     } else if (top) {  // instance leaf (:1870-1953)
       rec.rec(unit, rtf::TX_INSTANCE_LEAF);
+      uint32_t hdr_unit, broot_unit, broot_soff = 0;
       rtd::Instance in;
-      rtd::load_instance(g, saddr, in);
-      const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
-      if ((hdr & 63) || hdr / 64 >= v.n_units) {
-        status |= RT_RAY_BAD_NODE;
-        cn = on = 0;
-        return;
+      if (pinned) {
+        const uint4 h = rtd::ld_shared_v4(saddr);
+        hdr_unit = h.y;
+        broot_unit = h.z;
+        rbits = h.w & 0xffffu;
+        broot_soff = h.w >> 16;
+        float m[12];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const uint4 q = rtd::ld_shared_v4(saddr + rtp::IL_W2O + 16u * k);
+          m[4 * k + 0] = __uint_as_float(q.x);
+          m[4 * k + 1] = __uint_as_float(q.y);
+          m[4 * k + 2] = __uint_as_float(q.z);
+          m[4 * k + 3] = __uint_as_float(q.w);
+        }
+#pragma unroll
+        for (int k = 0; k < 12; ++k) in.w2o.m[k / 3][k % 3] = m[k];
+      } else {
+        rbits = __ldg(v.route + unit);
+        rtd::load_instance(g, saddr, in);
+        const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
+        if ((hdr & 63) || hdr / 64 >= v.n_units) return bad_node();
+        hdr_unit = (uint32_t)(hdr >> 6);
+        const uint4 h0 = __ldg(v.blob + (hdr >> 4));
+        const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
+        broot_unit = (uint32_t)(broot >> 6);
       }
-      rec.rec((uint32_t)(hdr >> 6), rtf::TX_STRUCTURE);
-      const uint4 h0 = __ldg(v.blob + (hdr >> 4));
-      const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
+      rec.rec(hdr_unit, rtf::TX_STRUCTURE);
       enter_instance(in, unit, O, D, tmin, tmax, ic);
       ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
-      route(a, (uint32_t)(broot >> 6) << 2, unit);
+      const uint32_t cc = broot_soff ? ((broot_soff << kEShift) | kEPin) : (broot_unit << kEShift);
+      push((rbits >> (kRouteInst + rsh)) & 1u, cc, unit);
     } else {  // primitive leaf (:2071-2196)
       rec.rec(unit, rtf::TX_LEAF_DESC);
       rtd::Node64 q;
@@ -176,7 +242,7 @@ struct Walker {
           c_leaf = unit;
           c_inst = inst;
           rec.rec(unit, rtf::TX_QUAD_LEAF_HIT);
-          if (terminate) cn = on = 0;
+          if (terminate) cu.n = ot.n = 0;
         } else {
           rec.rec(unit, rtf::TX_QUAD_LEAF);
         }
@@ -185,7 +251,7 @@ struct Walker {
         rec.rec(unit, rtf::TX_PROCEDURAL_LEAF);
       }
     }
-    if (status & RT_RAY_STACK_OVERFLOW) cn = on = 0;
+    if (status & RT_RAY_STACK_OVERFLOW) cu.n = ot.n = 0;
   }
 
   __device__ __forceinline__ void step(const TraceArgs& a) {
@@ -201,6 +267,8 @@ struct Walker {
 template <int CAP>
 __global__ void __launch_bounds__(256) trace_treelet_kernel(TraceArgs a) {
   Walker<CAP, false> w;
+  w.pin_base = 0;
+  w.pin_root = 0;
   unsigned long long bytes = 0;
   run_persistent(a, w, bytes);
   if (a.stats) add_warp_total64(a.stats + ST_NODE_BYTES, bytes);
@@ -257,6 +325,8 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
 
 constexpr int kMaxSlots = 8;  // slots per warp
 constexpr uint32_t kWaitTries = 1u << 22;
+constexpr int kStagedMaxThreads = 512;
+constexpr uint32_t kPinChunk = 32768;  // bytes per bulk copy of the pinned image
 
 // Per-warp staging state in shared memory.
 struct WarpStage {
@@ -267,25 +337,46 @@ struct WarpStage {
 };
 
 // The staged walk.  Persistent warps with ray refill (as run_persistent).
-// Every `epoch` node visits a warp votes: each lane names the treelet of its
-// next access, __match_any_sync counts equal names, and the most popular
-// treelet that is not resident (ties to the lowest treelet, i.e. the lowest
-// root address, as the RT unit's decision in shader.cc:3424-3441) is copied
-// with cp.async.bulk into the warp's least recently filled slot, provided at
-// least `min_votes` lanes want it.  A slot holds the first slot_bytes of the
-// treelet's image (the whole image when it fits).  Node reads that fall in a
-// resident slot are served from shared memory.  A slot is read only by its
-// own warp; __syncwarp orders the slot's reads before it is refilled.
-template <int CAP>
-__global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
+//
+// Pinned treelets: at launch each CTA copies the pinned image (the treelets
+// most rays visit, decoded into records, pinned.h) into shared memory with
+// cp.async.bulk and keeps it for the whole launch; every node read that names
+// a record is served from it.
+//
+// Warp slots: every `epoch` node visits a warp votes: each lane names the
+// treelet of its next access, __match_any_sync counts equal names, and the
+// most popular treelet that is not resident (ties to the lowest treelet, i.e.
+// the lowest root address, as the RT unit's decision in shader.cc:3424-3441)
+// is copied with cp.async.bulk into the warp's least recently filled slot,
+// provided at least `min_votes` lanes want it.  A slot holds the first
+// slot_bytes of the treelet's image (the whole image when it fits).  Node
+// reads that fall in a resident slot are served from shared memory.  A slot
+// is read only by its own warp; __syncwarp orders the slot's reads before it
+// is refilled.  SLOTS = false compiles the warp slots out (a.slots == 0).
+template <int CAP, bool SLOTS>
+__global__ void __launch_bounds__(kStagedMaxThreads) trace_staged_kernel(TraceArgs a) {
   extern __shared__ __align__(128) uint8_t dyn_smem[];
-  __shared__ WarpStage ws[8];
+  __shared__ WarpStage ws[kStagedMaxThreads / 32];
+  __shared__ uint64_t pin_bar;
+  __shared__ uint32_t pin_ok;
   uint8_t* const smem0 = dyn_smem + ((128u - (smem_u32(dyn_smem) & 127u)) & 127u);
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t slots = a.slots;
-  uint8_t* const my_slots = smem0 + (size_t)warp * slots * a.slot_bytes;
+  uint8_t* const my_slots = smem0 + a.pin_bytes + (size_t)warp * slots * a.slot_bytes;
   const uint32_t slot_base = smem_u32(my_slots);
   WarpStage& st = ws[warp];
+  if (threadIdx.x == 0) {
+    pin_ok = 0;
+    if (a.pin_bytes) {
+      mbar_init(&pin_bar, 1);
+      mbar_expect_tx(&pin_bar, a.pin_bytes);
+      for (uint32_t off = 0; off < a.pin_bytes; off += kPinChunk)
+        bulk_copy_g2s(smem0 + off, reinterpret_cast<const uint8_t*>(a.pin_image) + off,
+                      min(kPinChunk, a.pin_bytes - off), &pin_bar);
+      pin_ok = mbar_wait(&pin_bar, 0, kWaitTries) ? 1u : 0u;
+      if (!pin_ok) atomicOr(a.status, kStatusTimeout);
+    }
+  }
   if (lane == 0) {
     mbar_init(&st.bar, 1);
     for (int s = 0; s < kMaxSlots; ++s) {
@@ -299,7 +390,7 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
     st.victim = 0;
     st.disabled = 0;
   }
-  __syncwarp();
+  __syncthreads();
   // the node's location is read only while some slot of the warp is resident
   auto lookup = [&](uint32_t unit, const uint2* meta) -> uint32_t {
     bool any = false;
@@ -313,6 +404,8 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
     return 0u;
   };
   Walker<CAP, true> w;
+  w.pin_base = pin_ok ? smem_u32(smem0) : 0u;
+  w.pin_root = pin_ok ? a.pin_root : 0u;
   bool have = false, exhausted = false;
   uint32_t r = 0, it = 0;
   unsigned long long bytes = 0, staged = 0, stagings = 0, sreads = 0, greads = 0;
@@ -344,7 +437,7 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
       continue;
     }
     // --- staging: land a finished copy, then vote for the next one
-    if (slots > 0 && (it % a.epoch) == 0) {
+    if (SLOTS && slots > 0 && (it % a.epoch) == 0) {
       if (lane == 0 && st.pending_slot != kNone && mbar_test(&st.bar, st.phase)) {
         st.resident[st.pending_slot] = st.pending_id;
         st.units[st.pending_slot] = st.pending_units;
@@ -398,7 +491,8 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
     }
     // --- one node visit per lane
     if (have) {
-      w.step(a, lookup);
+      if (SLOTS) w.step(a, lookup);
+      else w.step(a);
       if (!w.active()) {
         w.finish(a, r);
         bytes += w.rec.bytes;
@@ -408,9 +502,12 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
       }
     }
   }
-  // a copy still in flight must land before the warp's shared memory goes away
+  // copies still in flight must land before the CTA's shared memory goes away
   if (lane == 0 && st.pending_slot != kNone) {
     if (!mbar_wait(&st.bar, st.phase, kWaitTries)) atomicOr(a.status, kStatusTimeout);
+  }
+  if (threadIdx.x == 0 && a.pin_bytes && !pin_ok) {
+    if (!mbar_wait(&pin_bar, 0, kWaitTries)) atomicOr(a.status, kStatusTimeout);
   }
   __syncwarp();
   if (a.stats) {
@@ -419,6 +516,11 @@ __global__ void __launch_bounds__(256) trace_staged_kernel(TraceArgs a) {
     add_warp_total64(a.stats + ST_GMEM_READS, greads);
     add_warp_total64(a.stats + ST_STAGED_BYTES, staged);
     add_warp_total64(a.stats + ST_STAGINGS, stagings);
+  }
+  if (a.stats && threadIdx.x == 0 && pin_ok && blockIdx.x == 0) {
+    // the pinned image counts once as staged bytes (copied by every CTA)
+    atomicAdd(a.stats + ST_STAGED_BYTES, (unsigned long long)a.pin_bytes * gridDim.x);
+    atomicAdd(a.stats + ST_STAGINGS, (unsigned long long)gridDim.x);
   }
 }
 

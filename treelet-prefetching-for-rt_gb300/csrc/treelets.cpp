@@ -19,6 +19,8 @@
 #include <unordered_map>
 
 #include "format.h"
+#include "pinned.h"
+#include "rtmath.h"
 
 namespace rtt {
 namespace {
@@ -227,6 +229,243 @@ void build_images(const uint8_t* blob, const Partition& p, std::vector<uint8_t>&
       pos += p.member_bytes[j];
     }
   }
+}
+
+void route_masks(const uint8_t* blob, uint64_t n_bytes, const Partition& p, std::vector<uint16_t>& out) {
+  const uint64_t n_units = n_bytes / 64;
+  out.assign(n_units, 0);
+  auto root_of = [&](uint32_t u) {
+    u &= kEntryUnitMask;
+    return u < n_units ? p.node_root[u] : kNoTreelet;
+  };
+  // bit `same` if the child shares u's root, bit `other` if its root is u
+  auto bits = [&](uint32_t u, uint32_t child, uint32_t same, uint32_t other) -> uint16_t {
+    const uint32_t rc = root_of(child);
+    uint16_t m = 0;
+    if (rc == p.node_root[u]) m |= (uint16_t)(1u << same);
+    if (rc == u) m |= (uint16_t)(1u << other);
+    return m;
+  };
+  // every unit a walk can pop: reachable internal nodes and instance leaves
+  std::vector<uint8_t> seen(n_units, 0);
+  std::vector<std::pair<uint32_t, uint8_t>> work;  // unit, kind (0 internal top, 1 internal bottom, 2 instance)
+  const uint64_t root_off = rd<uint64_t>(blob, rtf::HDR_ROOT_OFFSET);
+  if (root_off % 64 == 0 && root_off / 64 < n_units) work.push_back({(uint32_t)(root_off / 64), 0});
+  while (!work.empty()) {
+    const auto [u, kind] = work.back();
+    work.pop_back();
+    if (u >= n_units || seen[u] & (1u << kind)) continue;
+    seen[u] |= (uint8_t)(1u << kind);
+    const uint64_t off = (uint64_t)u * 64;
+    if (kind == 2) {
+      if (u + 1 >= n_units) continue;
+      const uint64_t hdr = off + rd<uint64_t>(blob, off + rtf::IL_BVH_ADDRESS);
+      if (hdr % 64 || hdr / 64 >= n_units) continue;
+      const uint64_t broot = hdr + rd<uint64_t>(blob, hdr + rtf::HDR_ROOT_OFFSET);
+      const uint32_t bu = (uint32_t)(broot >> 6);  // the walk's unit of the BLAS root
+      out[u] |= bits(u, bu, kRouteInstShift, kRouteInstShift + 1);
+      work.push_back({bu & kEntryUnitMask, 1});
+      continue;
+    }
+    // child units as the walk forms them: 32-bit node + offset, then + sizes
+    uint32_t c = (uint32_t)((int32_t)u + rd<int32_t>(blob, off + rtf::IN_CHILD_OFFSET));
+    for (int i = 0; i < 6; ++i) {
+      const uint8_t info = blob[off + rtf::IN_CHILD_INFO + i];
+      const uint32_t sz = rtf::child_size_units(info);
+      if (sz > 0) {
+        out[u] |= bits(u, c, i, kRouteOtherShift + i);
+        const bool internal = rtf::child_type(info) == rtf::CT_INTERNAL;
+        if (internal) work.push_back({c & kEntryUnitMask, kind});
+        else if (kind == 0) work.push_back({c & kEntryUnitMask, 2});
+      }
+      c += sz;
+    }
+  }
+}
+
+namespace {
+
+// Roles in which the walk can pop a unit.
+constexpr uint8_t kTopInternal = 1, kBotInternal = 2, kInstance = 4, kPrim = 8;
+
+// Breadth-first pass over every unit a walk can pop, from the TLAS root: the
+// roles each unit is reached in and, optionally, the node it was first
+// reached from (kNoTreelet for the root) and its surface-area visit
+// probability along that first path.
+void reach(const uint8_t* blob, uint64_t n_bytes, std::vector<uint8_t>& role, std::vector<double>* prob,
+           std::vector<uint32_t>* parent = nullptr) {
+  const uint64_t n_units = n_bytes / 64;
+  role.assign(n_units, 0);
+  if (prob) prob->assign(n_units, 0.0);
+  if (parent) parent->assign(n_units, kNoTreelet);
+  std::deque<uint32_t> q;
+  uint32_t from = kNoTreelet;
+  auto add = [&](uint32_t u, uint8_t r, double pr) {
+    u &= kEntryUnitMask;
+    if (u >= n_units || (r == kInstance && u + 1 >= n_units) || (role[u] & r)) return;
+    if (!role[u]) {
+      if (prob) (*prob)[u] = pr;
+      if (parent) (*parent)[u] = from;
+    }
+    role[u] |= r;
+    q.push_back(u);
+  };
+  const uint64_t root_off = rd<uint64_t>(blob, rtf::HDR_ROOT_OFFSET);
+  if (root_off % 64 == 0) add((uint32_t)(root_off / 64), kTopInternal, 1.0);
+  std::vector<uint8_t> done(n_units, 0);
+  while (!q.empty()) {
+    const uint32_t u = q.front();
+    from = u;
+    q.pop_front();
+    const uint8_t todo = role[u] & ~done[u];
+    done[u] |= todo;
+    const double pu = prob ? (*prob)[u] : 0.0;
+    const uint64_t off = (uint64_t)u * 64;
+    if (todo & kInstance) {
+      const uint64_t hdr = off + rd<uint64_t>(blob, off + rtf::IL_BVH_ADDRESS);
+      if (hdr % 64 == 0 && hdr / 64 < n_units) {
+        const uint64_t broot = hdr + rd<uint64_t>(blob, hdr + rtf::HDR_ROOT_OFFSET);
+        add((uint32_t)(broot >> 6), kBotInternal, pu);
+      }
+    }
+    for (uint8_t lvl : {kTopInternal, kBotInternal}) {
+      if (!(todo & lvl)) continue;
+      const float ox = rd<float>(blob, off + 0), oy = rd<float>(blob, off + 4), oz = rd<float>(blob, off + 8);
+      const float sx = rtm::exp2_int((int)(int8_t)blob[off + rtf::IN_EXP + 0] - 8);
+      const float sy = rtm::exp2_int((int)(int8_t)blob[off + rtf::IN_EXP + 1] - 8);
+      const float sz = rtm::exp2_int((int)(int8_t)blob[off + rtf::IN_EXP + 2] - 8);
+      double area[6] = {0, 0, 0, 0, 0, 0};
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int i = 0; i < 6; ++i) {
+        if (!rtf::child_size_units(blob[off + rtf::IN_CHILD_INFO + i])) continue;
+        const double l[3] = {ox + (double)blob[off + rtf::IN_LO_X + i] * sx, oy + (double)blob[off + rtf::IN_LO_Y + i] * sy,
+                             oz + (double)blob[off + rtf::IN_LO_Z + i] * sz};
+        const double h[3] = {ox + (double)blob[off + rtf::IN_HI_X + i] * sx, oy + (double)blob[off + rtf::IN_HI_Y + i] * sy,
+                             oz + (double)blob[off + rtf::IN_HI_Z + i] * sz};
+        const double dx = h[0] - l[0], dy = h[1] - l[1], dz = h[2] - l[2];
+        area[i] = dx * dy + dy * dz + dz * dx;
+        for (int a = 0; a < 3; ++a) {
+          lo[a] = std::min(lo[a], l[a]);
+          hi[a] = std::max(hi[a], h[a]);
+        }
+      }
+      const double ux = hi[0] - lo[0], uy = hi[1] - lo[1], uz = hi[2] - lo[2];
+      const double total = ux * uy + uy * uz + uz * ux;
+      uint32_t c = (uint32_t)((int32_t)u + rd<int32_t>(blob, off + rtf::IN_CHILD_OFFSET));
+      for (int i = 0; i < 6; ++i) {
+        const uint8_t info = blob[off + rtf::IN_CHILD_INFO + i];
+        const uint32_t size = rtf::child_size_units(info);
+        if (size > 0) {
+          const double pc = total > 0 ? pu * std::min(1.0, std::max(0.0, area[i] / total)) : pu;
+          const bool internal = rtf::child_type(info) == rtf::CT_INTERNAL;
+          add(c, internal ? lvl : (lvl == kTopInternal ? kInstance : kPrim), pc);
+        }
+        c += size;
+      }
+    }
+  }
+}
+
+template <class T>
+void put(std::vector<uint8_t>& b, uint64_t at, T v) {
+  std::memcpy(b.data() + at, &v, sizeof(T));
+}
+
+}  // namespace
+
+void default_pin_order(const uint8_t* blob, uint64_t n_bytes, std::vector<uint32_t>& order, const Partition& p) {
+  std::vector<uint8_t> role;
+  std::vector<double> prob;
+  reach(blob, n_bytes, role, &prob);
+  const uint32_t n = (uint32_t)p.roots.size();
+  std::vector<double> score(n);
+  for (uint32_t k = 0; k < n; ++k) score[k] = p.roots[k] == 0 ? 2.0 : prob[p.roots[k]];
+  order.resize(n);
+  for (uint32_t k = 0; k < n; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return score[a] > score[b]; });
+}
+
+void build_pinned(const uint8_t* blob, uint64_t n_bytes, const Partition& p, const std::vector<uint16_t>& route,
+                  const std::vector<uint32_t>& order, uint32_t budget, Pinned& out) {
+  out = Pinned();
+  budget = std::min<uint32_t>(budget, rtp::kMaxBytes) & ~127u;
+  if (budget < 256) return;
+  const uint64_t n_units = n_bytes / 64;
+  std::vector<uint8_t> role;
+  std::vector<uint32_t> parent;
+  reach(blob, n_bytes, role, nullptr, &parent);
+  auto rec_bytes = [&](uint8_t r) -> uint32_t {
+    if (r == kTopInternal || r == kBotInternal) return rtp::kInternalBytes;
+    if (r == kInstance) return rtp::kInstanceBytes;
+    if (r == kPrim) return rtp::kPrimBytes;
+    return 0;  // unreached, or reached in two roles: stays in global memory
+  };
+  // A record is only ever named by the record of its parent (or, for the
+  // root, by the launch), so a node is pinned only after its parent is; a
+  // treelet's members come in formation (breadth-first) order, so a treelet
+  // that does not fit whole leaves its top part pinned.
+  std::vector<uint32_t> soff(n_units, 0);
+  std::vector<uint32_t> recs;
+  std::vector<uint8_t> taken(p.roots.size(), 0);
+  uint32_t used = 16;  // soff 0 is no record
+  for (uint32_t k : order) {
+    if (k >= p.roots.size() || taken[k]) continue;
+    taken[k] = 1;
+    bool any = false;
+    for (uint64_t j = p.member_first[k]; j < p.member_first[k + 1]; ++j) {
+      const uint32_t u = p.members[j];
+      const uint32_t b = rec_bytes(role[u]);
+      if (soff[u] || !b || used + b > budget) continue;
+      if (parent[u] != kNoTreelet && !soff[parent[u]]) continue;
+      soff[u] = used / 16;
+      used += b;
+      recs.push_back(u);
+      any = true;
+    }
+    if (any) out.n_treelets++;
+    if (budget - used < 64) break;
+  }
+  if (recs.empty()) return;
+  out.bytes.assign((used + 127u) & ~127u, 0);
+  out.n_records = (uint32_t)recs.size();
+  auto soff_of = [&](uint32_t u) -> uint16_t {
+    u &= kEntryUnitMask;
+    return (uint16_t)(u < n_units ? soff[u] : 0);
+  };
+  for (uint32_t u : recs) {
+    const uint64_t at = (uint64_t)soff[u] * 16, off = (uint64_t)u * 64;
+    const uint8_t r = role[u];
+    if (r == kTopInternal || r == kBotInternal) {
+      std::memcpy(out.bytes.data() + at, blob + off, 64);
+      put<uint16_t>(out.bytes, at + rtp::IN_ROUTE, route[u]);
+      put<uint32_t>(out.bytes, at + rtp::IN_UNIT, u);
+      uint32_t c = (uint32_t)((int32_t)u + rd<int32_t>(blob, off + rtf::IN_CHILD_OFFSET));
+      for (int i = 0; i < 6; ++i) {
+        const uint32_t size = rtf::child_size_units(blob[off + rtf::IN_CHILD_INFO + i]);
+        if (size) put<uint16_t>(out.bytes, at + rtp::IN_CHILD_SOFF + 2 * i, soff_of(c));
+        c += size;
+      }
+    } else if (r == kInstance) {
+      const uint64_t hdr = off + rd<uint64_t>(blob, off + rtf::IL_BVH_ADDRESS);
+      const uint64_t broot = hdr + rd<uint64_t>(blob, hdr + rtf::HDR_ROOT_OFFSET);
+      const uint32_t bu = (uint32_t)(broot >> 6) & kEntryUnitMask;
+      put<uint32_t>(out.bytes, at + rtp::IL_UNIT, u);
+      put<uint32_t>(out.bytes, at + rtp::IL_HDR_UNIT, (uint32_t)(hdr >> 6));
+      put<uint32_t>(out.bytes, at + rtp::IL_BROOT_UNIT, bu);
+      put<uint16_t>(out.bytes, at + rtp::IL_ROUTE, route[u]);
+      put<uint16_t>(out.bytes, at + rtp::IL_ROUTE + 2, soff_of(bu));
+      for (int k = 0; k < 9; ++k)
+        put<float>(out.bytes, at + rtp::IL_W2O + 4 * k, rd<float>(blob, off + rtf::IL_W2O_LINEAR + 4 * k));
+      for (int k = 0; k < 3; ++k)
+        put<float>(out.bytes, at + rtp::IL_W2O + 36 + 4 * k, rd<float>(blob, off + rtf::IL_W2O_TRANSLATION + 4 * k));
+    } else {
+      std::memcpy(out.bytes.data() + at, blob + off, 64);
+      put<uint32_t>(out.bytes, at, u);
+    }
+  }
+  const uint64_t root_off = rd<uint64_t>(blob, rtf::HDR_ROOT_OFFSET);
+  const uint32_t ru = (uint32_t)(root_off >> 6) & kEntryUnitMask;
+  if (root_off % 64 == 0 && ru < n_units && role[ru] == kTopInternal) out.root_soff = soff[ru];
 }
 
 bool remap_layout(const Partition& p, uint64_t n_units, uint32_t stride, std::vector<uint64_t>& new_addr,

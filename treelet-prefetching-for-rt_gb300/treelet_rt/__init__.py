@@ -17,7 +17,7 @@ from ._ffi import (HIT_DTYPE, MODE_PLAIN, MODE_STAGED, MODE_TREELET, NO_TREELET,
                    RAY_FLAG_SKIP_CLOSEST_HIT, RAY_FLAG_TERMINATE_ON_FIRST_HIT, RAY_HIT_PROCEDURAL,
                    RAY_STACK_OVERFLOW, RAY_TRACE_OVERFLOW, SCENE_BLOBS, SCENE_CUBE, SCENE_CUBE_PLANE,
                    SCENE_SHARED_BLAS, SCENE_TERRAIN_INSTANCES, TX_BYTES, TX_NAMES, Camera, PrefetchParams,
-                   RTError, TraceBuf, TraceStats, TreeletInfo, Tuning, check, lib, ptr)
+                   TUNING_OFF, PinnedInfo, RTError, TraceBuf, TraceStats, TreeletInfo, Tuning, check, lib, ptr)
 
 __all__ = [
     "Blob", "Context", "Scene", "camera_rays", "default_camera", "bounce_rays_host", "RTError", "lib",
@@ -25,7 +25,7 @@ __all__ = [
     "RAY_FLAG_NO_OPAQUE", "RAY_FLAG_TERMINATE_ON_FIRST_HIT", "RAY_FLAG_SKIP_CLOSEST_HIT", "SCENE_CUBE_PLANE",
     "SCENE_TERRAIN_INSTANCES", "SCENE_BLOBS", "SCENE_CUBE", "SCENE_SHARED_BLAS", "TX_NAMES", "TX_BYTES",
     "NO_TREELET", "RAY_TRACE_OVERFLOW", "RAY_STACK_OVERFLOW", "RAY_HIT_PROCEDURAL", "RAY_BAD_NODE",
-    "PREFETCH_STATE_DTYPE", "PREFETCH_DECISION_DTYPE", "PrefetchParams", "unpack_visits",
+    "PREFETCH_STATE_DTYPE", "PREFETCH_DECISION_DTYPE", "PrefetchParams", "unpack_visits", "TUNING_OFF",
 ]
 
 
@@ -158,6 +158,23 @@ class Partition:
         check(lib().rt_partition_remap(self._h, stride, out.ctypes.data))
         return out
 
+    def route(self, blob: Blob) -> np.ndarray:
+        """Routing bits of the treelet-ordered walk, one uint16 per unit."""
+        out = np.zeros(self.n_units, np.uint16)
+        check(lib().rt_partition_route(self._h, blob.handle, out.ctypes.data))
+        return out
+
+    def pinned(self, blob: Blob, budget: int, order=None):
+        """The pinned-treelet image for `budget` bytes: (bytes, root record in 16-byte units)."""
+        o = None if order is None else np.ascontiguousarray(order, np.uint32)
+        n = C.c_uint64(0)
+        root = C.c_uint32(0)
+        args = (self._h, blob.handle, ptr(o), 0 if o is None else len(o), budget)
+        check(lib().rt_partition_pinned(*args, None, C.byref(n), C.byref(root)))
+        out = np.zeros(n.value, np.uint8)
+        check(lib().rt_partition_pinned(*args, out.ctypes.data, C.byref(n), C.byref(root)))
+        return out, root.value
+
 
 class Context:
     def __init__(self, device: int = 0):
@@ -241,10 +258,24 @@ class Scene:
         check(lib().rt_scene_set_stage_hints(self._h, h.ctypes.data))
 
     def set_tuning(self, block_threads=0, staged_threads=0, staged_epoch=0, staged_slots=0, refill_lanes=0,
-                   staged_slot_bytes=0, staged_min_votes=0, stack_depth=0) -> None:
+                   staged_slot_bytes=0, staged_min_votes=0, stack_depth=0, pinned_bytes=0) -> None:
+        """0 keeps a value; TUNING_OFF switches staged_slots / pinned_bytes off."""
         t = Tuning(block_threads, staged_threads, staged_epoch, staged_slots, refill_lanes, staged_slot_bytes,
-                   staged_min_votes, stack_depth)
+                   staged_min_votes, stack_depth, pinned_bytes)
         check(lib().rt_scene_set_tuning(self._h, C.byref(t)))
+
+    def set_pin_order(self, order=None) -> None:
+        """Dense treelet ids to pin first (None: the default order)."""
+        if order is None:
+            check(lib().rt_scene_set_pin_order(self._h, None, 0))
+            return
+        o = np.ascontiguousarray(order, np.uint32)
+        check(lib().rt_scene_set_pin_order(self._h, o.ctypes.data, len(o)))
+
+    def pinned_info(self) -> dict:
+        info = PinnedInfo()
+        check(lib().rt_scene_pinned_info(self._h, C.byref(info)))
+        return {k: getattr(info, k) for k, _ in PinnedInfo._fields_}
 
     def get_tuning(self) -> dict:
         t = Tuning()

@@ -52,7 +52,15 @@ class TreeletInfo(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("staged_threads", C.c_uint32), ("staged_epoch", C.c_uint32),
                 ("staged_slots", C.c_uint32), ("refill_lanes", C.c_uint32), ("staged_slot_bytes", C.c_uint32),
-                ("staged_min_votes", C.c_uint32), ("stack_depth", C.c_uint32)]
+                ("staged_min_votes", C.c_uint32), ("stack_depth", C.c_uint32), ("pinned_bytes", C.c_uint32)]
+
+
+TUNING_OFF = 0xFFFFFFFF
+
+
+class PinnedInfo(C.Structure):
+    _fields_ = [("bytes", C.c_uint32), ("n_treelets", C.c_uint32), ("n_records", C.c_uint32),
+                ("root_pinned", C.c_uint32)]
 
 
 class TraceStats(C.Structure):
@@ -104,6 +112,10 @@ PROTOTYPES = {
     "rt_partition_get": (C.c_int, [vp, vp, vp, vp, vp, vp]),
     "rt_partition_remap": (C.c_int, [vp, C.c_uint32, vp]),
     "rt_partition_free": (None, [vp]),
+    "rt_partition_route": (C.c_int, [vp, vp, vp]),
+    "rt_partition_pinned": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, vp, u64p, C.POINTER(C.c_uint32)]),
+    "rt_scene_set_pin_order": (C.c_int, [vp, vp, C.c_uint32]),
+    "rt_scene_pinned_info": (C.c_int, [vp, C.POINTER(PinnedInfo)]),
     "rt_trace_host_noalloc": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
     "rt_batch_create": (C.c_int, [vp, C.POINTER(vp), C.c_uint32, C.POINTER(vp)]),
     "rt_batch_destroy": (C.c_int, [vp]),
