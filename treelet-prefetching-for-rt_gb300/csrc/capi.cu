@@ -120,7 +120,7 @@ struct rt_scene {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
-  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, 98304};
+  rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096};
   // host-buffer path scratch
   cudaStream_t stream = nullptr;
   void* d_io = nullptr;

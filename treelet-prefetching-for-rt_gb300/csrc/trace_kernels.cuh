@@ -263,8 +263,7 @@ struct PlainWalker {
   bool opaque, terminate, inblas, fast;
   uint32_t next, c_leaf, c_inst, status;
   int sp;
-  uint32_t top;       // stack entry sp - 1, kept in a register
-  uint32_t stk[CAP];  // entries 0 .. sp - 2
+  uint32_t stk[CAP];
   InstCtx ic;
   bool ic_fast;
   Recorder rec;
@@ -273,22 +272,11 @@ struct PlainWalker {
   __device__ __forceinline__ bool active() const { return next != kNone || sp > 0; }
 
   __device__ __forceinline__ void push(uint32_t e) {
-    if (sp < CAP) {
-      if (sp > 0) stk[sp - 1] = top;
-      top = e;
-      ++sp;
-    } else {
-      status |= RT_RAY_STACK_OVERFLOW;
-    }
+    if (sp < CAP) stk[sp++] = e;
+    else status |= RT_RAY_STACK_OVERFLOW;
   }
 
-  // The refill of `top` is not needed until the next pop, so its load is off
-  // the path of the node visit that follows.
-  __device__ __forceinline__ uint32_t pop() {
-    const uint32_t e = top;
-    if (--sp > 0) top = stk[sp - 1];
-    return e;
-  }
+  __device__ __forceinline__ uint32_t pop() { return stk[--sp]; }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
     v = scene_of(a, r);
@@ -404,7 +392,7 @@ struct PlainWalker {
     for (;;) {
       if (next != kNone) return visit_internal(a, next);
       if (inblas) {
-        if (sp > 0 && !(top & kTop)) {
+        if (sp > 0 && !(stk[sp - 1] & kTop)) {
           const uint32_t e = pop();
           if (e & kLeaf) return visit_leaf(a, e >> 2);
           next = e >> 2;

@@ -14,26 +14,20 @@ constexpr uint32_t kSlotBitsDev = 10;
 constexpr uint32_t kEShift = 3, kEPin = 4;
 constexpr uint32_t kRouteOther = 6, kRouteInst = 12;  // route bits (treelets.h)
 
-// A LIFO stack whose top entry lives in a register: a pop takes the register
-// and reloads it from local memory, and that load is not needed until the
-// next pop, so it stays off the path of the node visit in between.
+// A LIFO stack of entries in local memory.  (Keeping the top entry in a
+// register measured slower on GB300: one more live 64-bit value per thread
+// costs more occupancy than the reload it saves.)
 template <int CAP>
 struct EStack {
-  unsigned long long top;
-  unsigned long long below[CAP];  // entries 0 .. n - 2
+  unsigned long long e[CAP];
   int n;
-  __device__ __forceinline__ bool push(unsigned long long e) {
+  __device__ __forceinline__ bool push(unsigned long long v) {
     if (n >= CAP) return false;
-    if (n > 0) below[n - 1] = top;
-    top = e;
-    ++n;
+    e[n++] = v;
     return true;
   }
-  __device__ __forceinline__ unsigned long long pop() {
-    const unsigned long long e = top;
-    if (--n > 0) top = below[n - 1];
-    return e;
-  }
+  __device__ __forceinline__ unsigned long long pop() { return e[--n]; }
+  __device__ __forceinline__ unsigned long long top() const { return e[n - 1]; }
 };
 
 // A ray's treelet-ordered walk.  Two LIFO stacks as in the reference
@@ -65,8 +59,8 @@ struct Walker {
   // next, i.e. its first pending access; kNone for a pinned node.
   __device__ __forceinline__ uint32_t next_loc() const {
     unsigned long long e;
-    if (cu.n > 0) e = cu.top;
-    else if (ot.n > 0) e = ot.top;
+    if (cu.n > 0) e = cu.top();
+    else if (ot.n > 0) e = ot.top();
     else return kNone;
     if ((uint32_t)e & kEPin) return kNone;
     const uint32_t unit = (uint32_t)e >> kEShift;

@@ -22,17 +22,25 @@ GRID_COMMON = {
     "refill_lanes": [4, 8, 16, 32],
     "stack_depth": [48, 96, 160],
 }
+OFF = 0xFFFFFFFF  # RT_TUNING_OFF
 GRID_STAGED = {
-    "staged_threads": [64, 128, 256],
+    "staged_threads": [128, 256, 512],
     "refill_lanes": [4, 8, 16, 32],
-    "staged_slots": [1, 2, 4],
+    "pinned_bytes": [OFF, 4096, 16384, 65536],
+    "staged_slots": [OFF, 1, 2, 4],
     "staged_slot_bytes": [1024, 2048, 4096, 65536],
     "staged_epoch": [4, 16, 64],
     "staged_min_votes": [2, 8],
     "stack_depth": [48, 96, 160],
 }
-DEFAULTS = {"block_threads": 128, "staged_threads": 128, "staged_epoch": 16, "staged_slots": 1, "refill_lanes": 8,
-            "staged_slot_bytes": 2048, "staged_min_votes": 2, "stack_depth": 96}
+DEFAULTS = {"block_threads": 128, "staged_threads": 256, "staged_epoch": 16, "staged_slots": OFF, "refill_lanes": 8,
+            "staged_slot_bytes": 2048, "staged_min_votes": 8, "stack_depth": 96, "pinned_bytes": 4096}
+
+
+def stages(cfg: dict) -> bool:
+    """True when a staged configuration moves treelets into shared memory at
+    all (pinned treelets or warp slots)."""
+    return cfg.get("pinned_bytes", OFF) != OFF or cfg.get("staged_slots", OFF) != OFF
 
 
 def time_trace(scene, d_rays, d_hits, n: int, mode: int, reps: int = 2, flush=None) -> float:
@@ -64,6 +72,8 @@ def _overflowed(d_hits, n: int) -> bool:
 
 def autotune(scene, d_rays, n: int, mode: int, budgets=None, reps: int = 2, passes: int = 2, flush=None,
              log=None) -> dict:
+    """Coordinate search; for the staged mode only configurations that stage
+    something (pinned treelets or warp slots) are candidates."""
     import torch
 
     import treelet_rt as rt
@@ -99,6 +109,8 @@ def autotune(scene, d_rays, n: int, mode: int, budgets=None, reps: int = 2, pass
                     continue
                 cand = dict(best)
                 cand[key] = v
+                if mode == rt.MODE_STAGED and not stages(cand):
+                    continue
                 ms = measure(cand)
                 if ms < best_ms:
                     best_ms, best = ms, cand
