@@ -588,6 +588,8 @@ def run_learned(args) -> None:
         hh = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
         scene.trace(rays_d, ref, rt.MODE_TREELET, n=n)
         apply_tuning(scene, "staged", name)
+        # the hints steer the warp-slot vote, so this comparison runs with slots on
+        scene.set_tuning(staged_slots=2, staged_min_votes=2, staged_epoch=8, staged_slot_bytes=8192)
         row = {}
         for label, h in (("heuristic_vote", None), ("learned_hints", hints)):
             scene.set_stage_hints(h)
@@ -614,6 +616,106 @@ def run_learned(args) -> None:
     scene.close()
 
 
+def run_replay(args) -> None:
+    """RT-unit trace replay (the trace consumer): a sample of the terrain
+    workload's rays (primary + bounce) traced in treelet order on the GPU, its
+    visit traces replayed through the RT-unit model with no prefetcher, the
+    treelet prefetcher (ALWAYS, POPULARITY, OMR / PMR schedulers, metadata
+    loads with and without the strict wait) and the Lee stride prefetcher.
+    Reports modeled cycles (the slowest unit), prefetch effectiveness, and the
+    replay's own speed on the GPU against the oracle on the host cores."""
+    import torch
+
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    rt.lib()
+    t0 = time.time()
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 1024 * 1024, SEED)
+    cam = rt.default_camera(rt.SCENE_TERRAIN_INSTANCES)
+    prim = rt.camera_rays(cam, 1024, 1024, 1, SEED, 1e-4, 1e30)
+    idx = np.random.default_rng(SEED).choice(len(prim), args.replay_rays // 2, replace=False)
+    idx.sort()
+    prim = prim[idx]
+    ctx = rt.Context(0)
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(BUDGET)
+    cap = 256
+    n_p = len(prim)
+    dp = torch.from_numpy(prim.view(np.uint8)).cuda()
+    hp = torch.empty(n_p * 64, dtype=torch.uint8, device="cuda")
+    scene.trace(dp, hp, rt.MODE_PLAIN, n=n_p)
+    db = torch.empty(n_p * 32, dtype=torch.uint8, device="cuda")
+    scene.bounce(dp, hp, db, seed=SEED + 100, n=n_p)
+    rays = torch.cat([dp, db])
+    n = 2 * n_p
+    hits = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+    vis = torch.zeros(n * cap, dtype=torch.int32, device="cuda")
+    scene.trace(rays, hits, rt.MODE_TREELET, visits=vis, capacity=cap, n=n)
+    torch.cuda.synchronize()
+    setup = time.time() - t0
+    base = dict(n_rt_units=args.rt_units, max_warps=16, l1_sets=32, l1_ways=16, hit_latency=20, miss_latency=300)
+    variants = {
+        "none": dict(),
+        "treelet_always": dict(prefetcher=1, heuristic=0),
+        "treelet_popularity_0.75": dict(prefetcher=1, heuristic=1, threshold=0.75),
+        "treelet_always_omr": dict(prefetcher=1, heuristic=0, scheduler=1),
+        "treelet_always_pmr": dict(prefetcher=1, heuristic=0, scheduler=2),
+        "treelet_always_metadata": dict(prefetcher=1, heuristic=0, load_metadata=1),
+        "treelet_always_metadata_wait": dict(prefetcher=1, heuristic=0, load_metadata=1, wait_metadata=1),
+        "stride_lee": dict(prefetcher=2, max_queue=0),
+    }
+    d_stats = torch.zeros(args.rt_units * rt.UNIT_STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    table = {}
+    gpu_s = {}
+    for name, extra in variants.items():
+        cfg = rt.unit_config(**base, **extra)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        scene.unit_replay(hits, vis, n, cap, cfg, d_stats)
+        gpu_s[name] = time.perf_counter() - t
+        s = np.frombuffer(d_stats.cpu().numpy().tobytes(), rt.UNIT_STATS_DTYPE)
+        pf = int(s["prefetch_issued"].sum())
+        eff = s["effectiveness"].sum(axis=0)
+        table[name] = {
+            "cycles": int(s["cycles"].max()), "demand_requests": int(s["demand_requests"].sum()),
+            "miss_rate": round(float(s["demand_misses"].sum() / max(1, s["demand_requests"].sum())), 4),
+            "hit_reserved_rate": round(float(s["demand_hit_reserved"].sum() / max(1, s["demand_requests"].sum())), 4),
+            "prefetch_issued": pf, "prefetch_queued": int(s["prefetch_queued"].sum()),
+            "effectiveness": {c: round(float(eff[i] / max(1, pf)), 4) for i, c in enumerate(rt.PF_CLASSES)},
+            "unclassified_but_accessed": round(float(s["unclassified_but_accessed"].sum() / max(1, pf)), 4),
+            "status": int(np.bitwise_or.reduce(s["status"])), "replay_s_gpu": round(gpu_s[name], 3)}
+    none_cycles = table["none"]["cycles"]
+    for row in table.values():
+        row["speedup_vs_none"] = round(none_cycles / max(1, row["cycles"]), 4)
+    # the replay's own speed: GPU (one thread per RT unit) against the oracle on all host cores
+    h = np.frombuffer(hits.cpu().numpy().tobytes(), rt.HIT_DTYPE)
+    v = vis.cpu().numpy().view(np.uint32).reshape(n, cap)
+    cfg = rt.unit_config(**base, **variants["treelet_always"])
+    threads = os.cpu_count() or 1
+    t = time.perf_counter()
+    exp = orc.unit_replay(orc.Treelets(blob.bytes(), BUDGET), h, v, cfg, threads=threads)
+    cpu_s = time.perf_counter() - t
+    scene.unit_replay(hits, vis, n, cap, cfg, d_stats)
+    got = np.frombuffer(d_stats.cpu().numpy().tobytes(), rt.UNIT_STATS_DTYPE)
+    equal = all(np.array_equal(got[f], exp[f]) for f in rt.UNIT_STATS_DTYPE.names)
+    reqs = int(exp["demand_requests"].sum() + exp["prefetch_issued"].sum())
+    line = {"metric": "modeled RT-unit cycles, treelet prefetching vs none (trace replay of GPU traces)",
+            "unit": "speedup", "value": table["treelet_always"]["speedup_vs_none"], "higher_is_better": True,
+            "n_gpus": 1,
+            "config": {"workload": f"terrain scene, {n_p} sampled primary rays + their bounce rays, treelet order, "
+                                   f"8 KiB treelets, visit traces of {cap} entries",
+                       "rt_units": args.rt_units, "max_warps": 16, "l1": "32 sets x 16 ways x 128 B (64 KiB), 32 B sectors",
+                       "latency": {"hit": 20, "miss": 300}, "setup_s": round(setup, 1)},
+            "variants": table,
+            "replay_speed": {"requests": reqs, "gpu_s": round(gpu_s["treelet_always"], 3), "cpu_s": round(cpu_s, 3),
+                             "cpu_threads": threads, "gpu_mrequests_s": round(reqs / gpu_s["treelet_always"] / 1e6, 3),
+                             "cpu_mrequests_s": round(reqs / cpu_s / 1e6, 3), "stats_equal_oracle": bool(equal)},
+            "dtype": "u32/u64 (model)", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+    scene.close()
+
+
 def C_void(v: int):
     import ctypes
 
@@ -630,12 +732,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="small: the same scene with 512x512x1 primary rays + bounces (profiling case)")
-    ap.add_argument("--workload", default="terrain", choices=["terrain", "ao", "batch", "learned"],
+    ap.add_argument("--workload", default="terrain", choices=["terrain", "ao", "batch", "learned", "replay"],
                     help="terrain: the headline line; ao: AO budget sweep; batch: many scenes in one launch; "
-                         "learned: the learned prefetcher against the heuristic")
+                         "learned: the learned prefetcher against the heuristic; replay: RT-unit trace replay")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--train-steps", type=int, default=6000)
+    ap.add_argument("--replay-rays", type=int, default=65536)
+    ap.add_argument("--rt-units", type=int, default=32)
     args = ap.parse_args()
+    if args.workload == "replay" and args.impl != "reference":
+        return run_replay(args)
     if args.workload == "learned" and args.impl != "reference":
         return run_learned(args)
     if args.workload == "ao" and args.impl != "reference":

@@ -429,6 +429,86 @@ rt_status rt_prefetch_decide(rt_scene* scene, const uint32_t* next_unit, uint32_
                              const rt_prefetch_params* params, rt_prefetch_state* state, rt_prefetch_decision* out,
                              void* stream);
 
+/* ---------------- RT-unit trace replay ---------------- */
+
+/* Replays the visit traces of a traced batch through a model of the
+ * reference's RT units and their treelet prefetching, with no reference
+ * counterpart as one call: it restates the RT unit's request loop
+ * (shader.cc:4394-4450, one 32-byte request per cycle, prefetches only on
+ * cycles without a demand request, shader.cc:4118-4130, :4453-4501), warp
+ * selection (treelet_scheduler 0/1/2, shader.cc:4307-4392), the
+ * treelet-prefetch decision every prefetch_delay cycles (shader.cc:3419-3683,
+ * with the metadata loads of load_treelet_metadata and the strict wait of
+ * wait_for_metadata_load), the Lee MICRO'10 stride prefetcher
+ * (shader.cc:4792-4826), the removal of queued prefetches a demand request
+ * covers (shader.cc:4657-4681, :4765-4790), and the prefetch classification
+ * of gpu-cache.cc:1953-2116 with the final tally of gpu-sim.cc:1749-1790.
+ * The memory behind it is this library's own simple model: one sectored L1
+ * per RT unit (128 B lines, 32 B sectors, LRU), a fixed hit latency and a
+ * fixed miss latency, merging of requests to a sector in flight.
+ *
+ * Warp w (rays 32w .. 32w + 31 of the batch) runs on RT unit w % n_rt_units,
+ * units take their warps in order, at most max_warps at a time.  A warp
+ * issues, per round, the next transaction of each lane that has one
+ * (identical (address, size) pairs once), split into 32 B requests; the
+ * round completes when its last request's data is back, plus the longest
+ * intersection latency of its transaction types (2,4,4,2,4,4,4 cycles by
+ * transaction type, -gpgpu_rt_intersection_latency).  Transaction addresses
+ * are unit * 64 with the sizes of rt_trace's visit entries.  Treelet k's
+ * metadata (max_treelet_bytes / 16 bytes, vulkan_ray_tracing.cc:1601-1602)
+ * sits at (blob bytes rounded up to 4 KiB) + k * that size; a member that is
+ * not a treelet root loads treelet 0's, as the reference's map lookup does. */
+#define RT_UNIT_PF_NONE 0u
+#define RT_UNIT_PF_TREELET 1u
+#define RT_UNIT_PF_STRIDE 2u   /* Lee MICRO'10 */
+#define RT_UNIT_SCHED_FIRST 0u /* first ready warp (treelet_scheduler 0) */
+#define RT_UNIT_SCHED_OMR 1u   /* first ready warp with a lane headed into the last prefetched treelet */
+#define RT_UNIT_SCHED_PMR 2u   /* ready warp with the most such lanes */
+typedef struct rt_unit_config {
+  uint32_t n_rt_units;       /* RT units */
+  uint32_t max_warps;        /* resident warps per unit (-gpgpu_rt_max_warps, 1..16) */
+  uint32_t l1_sets;          /* L1 sets (power of two) */
+  uint32_t l1_ways;          /* L1 ways (1..32) */
+  uint32_t hit_latency;      /* cycles from request to data on a hit (>= 1) */
+  uint32_t miss_latency;     /* cycles from request to data on a miss (>= 1, <= 4096) */
+  uint32_t prefetcher;       /* RT_UNIT_PF_* */
+  uint32_t scheduler;        /* RT_UNIT_SCHED_* (OMR / PMR need the treelet prefetcher) */
+  rt_prefetch_params decision; /* treelet prefetcher: heuristic, max queue, threshold, second prefetch */
+  uint32_t prefetch_delay;   /* cycles between decisions (>= 1) */
+  uint32_t load_metadata;    /* queue each member's treelet metadata before it (-load_treelet_metadata) */
+  uint32_t wait_metadata;    /* strict wait for the metadata (-wait_for_metadata_load) */
+  uint32_t max_cycles;       /* per unit, 0 = no limit */
+} rt_unit_config;
+
+/* Effectiveness classes, numbered as prefetch_request_effectiveness
+ * (abstract_hardware_model.h:247-254). */
+#define RT_PF_TOO_LATE 0u
+#define RT_PF_LATE 1u
+#define RT_PF_TIMELY 2u
+#define RT_PF_TOO_EARLY 3u
+#define RT_PF_NEVER_USED 4u
+
+typedef struct rt_unit_stats {
+  uint64_t cycles;              /* cycle after the unit's last warp left */
+  uint64_t warps, transactions; /* warps run, lane transactions consumed */
+  uint64_t demand_requests;     /* 32 B demand requests */
+  uint64_t demand_hits, demand_hit_reserved, demand_misses;
+  uint64_t prefetch_queued, prefetch_issued, prefetch_removed; /* 32 B prefetch requests */
+  uint64_t prefetch_present, prefetch_merged, prefetch_filled; /* what an issued prefetch found */
+  uint64_t decisions, treelets_prefetched, metadata_queued;
+  uint64_t effectiveness[5];         /* RT_PF_* tally at the end */
+  uint64_t unclassified_but_accessed;
+  uint64_t status;              /* bit 0: a model table filled up; bit 1: max_cycles reached */
+} rt_unit_stats;
+
+/* hits / visits are the device outputs of rt_trace on `n` rays (visits with
+ * `capacity` entries per ray; a ray replays min(n_visits, capacity) of them).
+ * stats: device array of n_rt_units records.  Needs rt_treelets_form.  One
+ * CUDA thread models one RT unit; the call allocates the units' tables,
+ * synchronises `stream` and frees them before it returns. */
+rt_status rt_unit_replay(rt_scene* scene, const rt_hit* hits, const uint32_t* visits, uint32_t n, uint32_t capacity,
+                         const rt_unit_config* config, rt_unit_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

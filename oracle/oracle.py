@@ -67,6 +67,8 @@ def lib():
         L.oracle_prefetch_decide.argtypes = [vp, vp, C.c_uint32, C.POINTER(_Params), vp, vp]
         L.oracle_decode_node.restype = C.c_int
         L.oracle_decode_node.argtypes = [vp, C.c_uint32, C.c_int, vp]
+        L.oracle_unit_replay.restype = C.c_int
+        L.oracle_unit_replay.argtypes = [vp, C.c_int, C.c_uint64, vp, vp, C.c_uint32, C.c_uint32, vp, vp, C.c_int]
         _lib = L
     return _lib
 
@@ -145,6 +147,22 @@ def trace(blob: np.ndarray, rays: np.ndarray, mode: int = 0, treelets: Treelets 
     if rc != 0:
         raise OracleError(lib().oracle_last_error().decode())
     return hits, vis, tl
+
+
+def unit_replay(treelets: Treelets, hits: np.ndarray, visits: np.ndarray, config, threads: int = 8) -> np.ndarray:
+    """RT-unit replay of a traced batch (`config`: a treelet_rt UnitConfig);
+    returns config.n_rt_units stats records (treelet_rt.UNIT_STATS_DTYPE layout)."""
+    from treelet_rt import UNIT_STATS_DTYPE
+
+    hits = np.ascontiguousarray(hits, HIT_DTYPE)
+    visits = np.ascontiguousarray(visits, np.uint32)
+    n, cap = visits.shape
+    out = np.zeros(config.n_rt_units, UNIT_STATS_DTYPE)
+    rc = lib().oracle_unit_replay(treelets.h, treelets.max_bytes, treelets.blob.nbytes, hits.ctypes.data,
+                                  visits.ctypes.data, n, cap, C.byref(config), out.ctypes.data, threads)
+    if rc != 0:
+        raise OracleError(lib().oracle_last_error().decode())
+    return out
 
 
 def prefetch_decide(treelets: Treelets, next_unit: np.ndarray, heuristic: int = 0, max_queue: int = 1000000,

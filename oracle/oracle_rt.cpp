@@ -1096,3 +1096,436 @@ int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- RT-unit replay
+
+namespace {
+
+enum Effectiveness { E_TOO_LATE = 0, E_LATE, E_TIMELY, E_TOO_EARLY, E_NEVER_USED, E_UNCLASSIFIED };
+
+struct PrefetchRecord {  // prefetch_block_info (gpu-cache.h:99-113), the fields the classification reads
+  uint64_t block;        // 32 B sector address (the sector cache's MSHR address)
+  int effectiveness = E_UNCLASSIFIED;
+};
+
+struct SectorState {
+  bool valid = false;
+  uint64_t ready = 0;  // cycle the data is there
+  bool by_prefetch = false;
+  int64_t record = -1;  // the prefetch record that filled it
+};
+
+struct CacheLine {
+  bool used = false;
+  uint64_t block = 0;  // 128 B line address
+  uint64_t lru = 0;
+  SectorState s[4];
+};
+
+struct Request {
+  uint64_t addr, base;
+  bool first_of_tx;
+};
+
+struct LaneTrace {
+  const uint32_t* row = nullptr;
+  uint32_t ptr = 0, end = 0;
+  bool issued = false;
+};
+
+struct UnitWarp {
+  uint32_t wid = 0;  // warp id of the stride tables
+  LaneTrace lane[32];
+  bool in_flight = false, all_sent = false;
+  uint64_t ready = 0;
+  uint32_t ilat = 0;
+  bool done() const {
+    for (const auto& l : lane)
+      if (l.ptr < l.end) return false;
+    return true;
+  }
+};
+
+constexpr uint32_t kIntersectionLatency[7] = {2, 4, 4, 2, 4, 4, 4};  // -gpgpu_rt_intersection_latency
+
+uint32_t tx_size(uint32_t type) { return type == 2 ? 128u : (type == 3 ? 8u : 64u); }
+
+struct UnitReplay {
+  const oracle_treelets* tl;
+  const rt_unit_config& cfg;
+  uint64_t meta_base, meta_size, n_treelets;
+  std::map<const uint8_t*, int> metadata_idx;  // treelet_addr_to_metadata_idx
+  rt_unit_stats st{};
+  std::vector<CacheLine> lines;
+  std::vector<PrefetchRecord> records;
+  std::map<uint64_t, int64_t> last_evicted;  // sector -> most recently evicted prefetch record
+  std::deque<std::pair<uint64_t, uint64_t>> pq;  // prefetch_mem_access_q: (request, base)
+  std::deque<Request> chunk_q;                 // mem_access_q of the warp being served
+  UnitWarp* serving = nullptr;
+  std::list<UnitWarp> resident;                // m_current_warps, oldest first
+  std::deque<std::pair<uint64_t, uint64_t>> metadata_returns;  // (cycle, base)
+  uint64_t most_recent_metadata = 0;
+  rt_prefetch_state dstate{0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0};
+  std::map<uint32_t, std::map<int, int>> pws_table;  // Lee: warp -> stride -> count
+  std::map<uint32_t, uint64_t> pws_last;
+
+  UnitReplay(const oracle_treelets* t, const rt_unit_config& c) : tl(t), cfg(c) {}
+
+  const uint8_t* root_of_addr(uint64_t a) const { return tl->addrToTreeletID(tl->base + a); }
+
+  CacheLine* find(uint64_t block) {
+    const uint64_t set = block & (cfg.l1_sets - 1);
+    for (uint32_t w = 0; w < cfg.l1_ways; ++w) {
+      CacheLine& l = lines[set * cfg.l1_ways + w];
+      if (l.used && l.block == block) return &l;
+    }
+    return nullptr;
+  }
+
+  // Allocates the line for `block` (an unused way first, else the least
+  // recently used, lowest way on ties), recording evicted prefetched sectors.
+  CacheLine* allocate(uint64_t block, uint64_t t) {
+    const uint64_t set = block & (cfg.l1_sets - 1);
+    CacheLine* victim = nullptr;
+    for (uint32_t w = 0; w < cfg.l1_ways && !victim; ++w)
+      if (!lines[set * cfg.l1_ways + w].used) victim = &lines[set * cfg.l1_ways + w];
+    if (!victim) {
+      for (uint32_t w = 0; w < cfg.l1_ways; ++w) {
+        CacheLine& l = lines[set * cfg.l1_ways + w];
+        if (!victim || l.lru < victim->lru) victim = &l;
+      }
+      for (int k = 0; k < 4; ++k)
+        if (victim->s[k].valid && victim->s[k].by_prefetch) last_evicted[victim->block * 4 + k] = victim->s[k].record;
+    }
+    *victim = CacheLine();
+    victim->used = true;
+    victim->block = block;
+    victim->lru = t;
+    return victim;
+  }
+
+  uint64_t demand(uint64_t addr, uint64_t t) {
+    const uint64_t sector = addr >> 5, block = addr >> 7;
+    const int k = (int)((addr >> 5) & 3);
+    st.demand_requests++;
+    CacheLine* l = find(block);
+    if (l && l->s[k].valid) {
+      l->lru = t;
+      SectorState& s = l->s[k];
+      if (s.ready <= t) {  // HIT
+        st.demand_hits++;
+        if (s.by_prefetch && records[s.record].effectiveness == E_UNCLASSIFIED) records[s.record].effectiveness = E_TIMELY;
+        return t + cfg.hit_latency;
+      }
+      st.demand_hit_reserved++;  // HIT_RESERVED
+      if (s.by_prefetch && records[s.record].effectiveness == E_UNCLASSIFIED) records[s.record].effectiveness = E_LATE;
+      return s.ready;
+    }
+    st.demand_misses++;  // MISS / SECTOR_MISS
+    auto ev = last_evicted.find(sector);
+    if (ev != last_evicted.end() && records[ev->second].effectiveness == E_UNCLASSIFIED)
+      records[ev->second].effectiveness = E_TOO_EARLY;
+    if (!l) l = allocate(block, t);
+    l->lru = t;
+    l->s[k] = SectorState{true, t + cfg.miss_latency, false, -1};
+    return t + cfg.miss_latency;
+  }
+
+  void prefetch(uint64_t addr, uint64_t base, uint64_t t) {
+    const uint64_t block = addr >> 7;
+    const int k = (int)((addr >> 5) & 3);
+    const int64_t id = (int64_t)records.size();
+    records.push_back(PrefetchRecord{addr >> 5});
+    st.prefetch_issued++;
+    CacheLine* l = find(block);
+    if (l && l->s[k].valid) {
+      l->lru = t;
+      if (l->s[k].ready <= t) {
+        st.prefetch_present++;
+        // gpu-cache.cc:2101-2116: only a record already classified becomes TOO_LATE
+        if (!l->s[k].by_prefetch && records[id].effectiveness != E_UNCLASSIFIED) records[id].effectiveness = E_TOO_LATE;
+      } else {
+        st.prefetch_merged++;
+      }
+      return;
+    }
+    st.prefetch_filled++;
+    if (!l) l = allocate(block, t);
+    l->lru = t;
+    l->s[k] = SectorState{true, t + cfg.miss_latency, true, id};
+    if (is_metadata(base)) metadata_returns.emplace_back(t + cfg.miss_latency, base);
+  }
+
+  bool is_metadata(uint64_t base) const {
+    return cfg.load_metadata && base >= meta_base && base <= meta_base + n_treelets * meta_size;
+  }
+
+  uint64_t metadata_addr(const uint8_t* root) {
+    return meta_base + (uint64_t)metadata_idx[root] * meta_size;  // operator[]: 0 for a non-root
+  }
+
+  // Removes queued prefetches of this address, stepping past the entry that
+  // follows each erased one (shader.cc:4657-4668 as written).
+  void remove_queued(uint64_t addr) {
+    for (size_t idx = 0; idx < pq.size(); idx++) {
+      if (addr == pq[idx].first) {
+        pq.erase(pq.begin() + (long)idx);
+        st.prefetch_removed++;
+      }
+    }
+  }
+
+  void push_member(const StackEntry& m, bool with_metadata) {
+    if (with_metadata && cfg.load_metadata) {
+      const uint64_t ma = meta_base + (uint64_t)metadata_idx[m.addr] * meta_size;
+      for (uint64_t i = 0; i < meta_size / 32; ++i) {
+        pq.emplace_back(ma + i * 32, ma);
+        st.metadata_queued++;
+        st.prefetch_queued++;
+      }
+    }
+    const uint64_t a = (uint64_t)(m.addr - tl->base);
+    for (int i = 0; i < (m.size + 31) / 32; ++i) {
+      pq.emplace_back(a + 32ull * i, a);
+      st.prefetch_queued++;
+    }
+  }
+
+  // Lee MICRO'10 (shader.cc:4792-4826 as written: the last address is only
+  // recorded on a warp's first access; prefetches are queued only while the
+  // queue holds at least max_prefetch_queue_size entries).
+  void stride_prefetch(uint32_t wid, uint64_t next_addr) {
+    if (pws_table.count(wid) == 0) {
+      pws_last[wid] = next_addr;
+    } else if (pws_table[wid].size() <= 32) {
+      const int stride = (int)(uint32_t)(next_addr - pws_last[wid]);
+      pws_table[wid][stride]++;
+    }
+    int largest_stride = 0, largest_count = 0;
+    for (auto& kv : pws_table[wid])
+      if (kv.second > largest_count) {
+        largest_stride = kv.first;
+        largest_count = kv.second;
+      }
+    const uint64_t pa = next_addr + (uint64_t)(int64_t)largest_stride;
+    if (cfg.decision.max_queue <= pq.size()) {
+      for (unsigned i = 0; i < 2; ++i) {
+        pq.emplace_back(pa + i * 32, pa);
+        st.prefetch_queued++;
+      }
+    }
+  }
+
+  void decide() {
+    std::vector<uint32_t> next;
+    for (auto& w : resident)
+      for (auto& l : w.lane) next.push_back(l.ptr < l.end ? (l.row[l.ptr] >> 3) : 0xFFFFFFFFu);
+    dstate.queue_len = (uint32_t)pq.size();
+    rt_prefetch_decision d;
+    oracle_prefetch_decide(tl, next.data(), (uint32_t)next.size(), &cfg.decision, &dstate, &d);
+    st.decisions++;
+    if (d.submitted) {
+      const auto& nodes = tl->roots.at(tl->base + (uint64_t)d.treelet * 64);
+      for (uint32_t j = d.first_member; j < d.first_member + d.n_members; ++j) push_member(nodes[j], true);
+      st.treelets_prefetched++;
+    }
+    if (d.second_treelet != 0xFFFFFFFFu) {
+      for (const auto& m : tl->roots.at(tl->base + (uint64_t)d.second_treelet * 64)) push_member(m, false);
+      st.treelets_prefetched++;
+    }
+  }
+
+  // rt_unit::schedule_next_warp (shader.cc:4307-4392)
+  UnitWarp* schedule() {
+    auto ready = [](const UnitWarp& w) { return !w.in_flight && !w.done(); };
+    const bool treelet = cfg.prefetcher == RT_UNIT_PF_TREELET;
+    auto matches = [&](const UnitWarp& w) {
+      int c = 0;
+      for (const auto& l : w.lane)
+        if (l.ptr < l.end) {
+          const uint8_t* r = root_of_addr((uint64_t)(l.row[l.ptr] >> 3) * 64);
+          if (dstate.last_prefetched != 0xFFFFFFFFu && r == tl->base + (uint64_t)dstate.last_prefetched * 64) ++c;
+        }
+      return c;
+    };
+    if (treelet && cfg.scheduler == RT_UNIT_SCHED_OMR) {
+      for (auto& w : resident)
+        if (ready(w) && matches(w) > 0) return &w;
+    } else if (treelet && cfg.scheduler == RT_UNIT_SCHED_PMR) {
+      UnitWarp* best = nullptr;
+      int best_count = 0;
+      for (auto& w : resident)
+        if (ready(w)) {
+          const int c = matches(w);
+          if (c > best_count) {
+            best = &w;
+            best_count = c;
+          }
+        }
+      if (best) return best;
+    }
+    for (auto& w : resident)
+      if (ready(w)) return &w;
+    return nullptr;
+  }
+
+  void start_round(UnitWarp* w) {
+    std::vector<std::pair<uint64_t, uint32_t>> seen;  // m_next_rt_accesses_set: (address, size)
+    uint32_t ilat = 0;
+    for (auto& l : w->lane) {
+      l.issued = l.ptr < l.end;
+      if (!l.issued) continue;
+      const uint32_t v = l.row[l.ptr];
+      const uint64_t a = (uint64_t)(v >> 3) * 64;
+      const uint32_t size = tx_size(v & 7);
+      ilat = std::max(ilat, kIntersectionLatency[v & 7]);
+      bool dup = false;
+      for (auto& p : seen)
+        if (p.first == a && p.second == size) dup = true;
+      if (dup) continue;
+      seen.emplace_back(a, size);
+      for (uint32_t i = 0; i < (size + 31) / 32; ++i) chunk_q.push_back(Request{a + 32ull * i, a, i == 0});
+    }
+    w->in_flight = true;
+    w->all_sent = false;
+    w->ready = 0;
+    w->ilat = ilat;
+    serving = w;
+  }
+
+  void send_demand(uint64_t t) {
+    const Request r = chunk_q.front();
+    chunk_q.pop_front();
+    if (cfg.prefetcher == RT_UNIT_PF_TREELET || cfg.prefetcher == RT_UNIT_PF_STRIDE) remove_queued(r.addr);
+    if (cfg.prefetcher == RT_UNIT_PF_STRIDE && r.first_of_tx) stride_prefetch(serving->wid, r.addr);
+    const uint64_t ret = demand(r.addr, t);
+    serving->ready = std::max(serving->ready, ret);
+    if (chunk_q.empty()) {
+      serving->all_sent = true;
+      serving->ready += serving->ilat;
+      serving = nullptr;
+    }
+  }
+
+  bool prefetch_issuable() {
+    const uint64_t base = pq.front().second;
+    if (!cfg.wait_metadata || is_metadata(base)) return true;
+    return most_recent_metadata == metadata_addr(root_of_addr(base));  // shader.cc:4469-4476
+  }
+
+  void run(std::vector<uint32_t> warps, const rt_hit* hits, const uint32_t* visits, uint32_t n, uint32_t capacity) {
+    lines.assign((size_t)cfg.l1_sets * cfg.l1_ways, CacheLine());
+    size_t next_warp = 0;
+    uint32_t local = 0;
+    for (uint64_t t = 0;; ++t) {
+      for (auto it = resident.begin(); it != resident.end();) {
+        if (it->in_flight && it->all_sent && it->ready <= t) {
+          for (auto& l : it->lane)
+            if (l.issued) {
+              l.ptr++;
+              l.issued = false;
+              st.transactions++;
+            }
+          it->in_flight = false;
+        }
+        if (!it->in_flight && it->done()) {
+          st.warps++;
+          it = resident.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      while (resident.size() < cfg.max_warps && next_warp < warps.size()) {
+        UnitWarp w;
+        const uint32_t g = warps[next_warp++];
+        w.wid = local++ % cfg.max_warps;
+        for (uint32_t i = 0; i < 32; ++i) {
+          const uint64_t r = (uint64_t)g * 32 + i;
+          if (r < n) {
+            w.lane[i].row = visits + r * capacity;
+            w.lane[i].end = std::min(hits[r].n_visits, capacity);
+          }
+        }
+        resident.push_back(w);
+      }
+      if (resident.empty()) {
+        st.cycles = t;
+        break;
+      }
+      if (cfg.max_cycles && t >= cfg.max_cycles) {
+        st.cycles = t;
+        st.status |= 2;
+        break;
+      }
+      while (!metadata_returns.empty() && metadata_returns.front().first <= t) {
+        most_recent_metadata = metadata_returns.front().second;
+        metadata_returns.pop_front();
+      }
+      if (cfg.prefetcher == RT_UNIT_PF_TREELET && t % cfg.prefetch_delay == 0) decide();
+      if (!chunk_q.empty()) {
+        send_demand(t);
+      } else if (UnitWarp* w = schedule()) {
+        start_round(w);
+        send_demand(t);
+      } else if (cfg.prefetcher != RT_UNIT_PF_NONE && !pq.empty() && prefetch_issuable()) {
+        const auto req = pq.front();
+        pq.pop_front();
+        prefetch(req.first, req.second, t);
+      }
+    }
+    // final tally (gpu-sim.cc:1749-1790)
+    std::map<uint64_t, std::vector<PrefetchRecord*>> by_block;
+    for (auto& r : records) by_block[r.block].push_back(&r);
+    for (auto& kv : by_block) {
+      bool accessed = false;
+      for (auto* r : kv.second)
+        if (r->effectiveness != E_UNCLASSIFIED && r->effectiveness != E_NEVER_USED) accessed = true;
+      for (auto* r : kv.second) {
+        if (accessed) {
+          if (r->effectiveness == E_UNCLASSIFIED) {
+            st.unclassified_but_accessed++;
+            continue;
+          }
+        } else if (r->effectiveness == E_UNCLASSIFIED) {
+          r->effectiveness = E_NEVER_USED;
+        }
+        st.effectiveness[r->effectiveness]++;
+      }
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" int oracle_unit_replay(const oracle_treelets* tl, int max_treelet_bytes, uint64_t blob_bytes,
+                                  const rt_hit* hits, const uint32_t* visits, uint32_t n, uint32_t capacity,
+                                  const rt_unit_config* cfg, rt_unit_stats* stats, int threads) {
+  if (!tl || !cfg || !stats || cfg->n_rt_units == 0 || cfg->max_warps == 0 || cfg->l1_sets == 0 ||
+      cfg->l1_ways == 0 || cfg->prefetch_delay == 0) {
+    fail_msg("oracle_unit_replay: bad arguments");
+    return -1;
+  }
+  std::map<const uint8_t*, int> idx;
+  int k = 0;
+  for (auto& kv : tl->roots) idx[kv.first] = k++;
+  const uint32_t n_warps = (n + 31) / 32;
+  auto one = [&](uint32_t u) {
+    UnitReplay r(tl, *cfg);
+    r.meta_base = (blob_bytes + 4095) & ~4095ull;
+    r.meta_size = (uint64_t)(max_treelet_bytes / 64) * 4;
+    r.n_treelets = tl->roots.size();
+    r.metadata_idx = idx;
+    std::vector<uint32_t> warps;
+    for (uint32_t w = u; w < n_warps; w += cfg->n_rt_units) warps.push_back(w);
+    r.run(warps, hits, visits, n, capacity);
+    stats[u] = r.st;
+  };
+  const int nt = std::max(1, std::min<int>(threads, (int)cfg->n_rt_units));
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nt; ++i)
+    pool.emplace_back([&, i] {
+      for (uint32_t u = (uint32_t)i; u < cfg->n_rt_units; u += (uint32_t)nt) one(u);
+    });
+  for (auto& th : pool) th.join();
+  return 0;
+}

@@ -60,6 +60,16 @@ int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* t
 int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
                            const rt_prefetch_params* p, rt_prefetch_state* state, rt_prefetch_decision* out);
 
+/* The RT-unit trace replay of rt_unit_replay (treelet_rt.h), restated with
+ * the reference's containers: a std::deque prefetch queue erased in place,
+ * per-block vectors of prefetch records classified as gpu-cache.cc:1953-2116
+ * does, std::map histograms through oracle_prefetch_decide, std::map stride
+ * tables.  max_treelet_bytes sizes the metadata (vulkan_ray_tracing.cc:1601-1602).
+ * stats: n_rt_units records.  Returns 0 or -1. */
+int oracle_unit_replay(const oracle_treelets* tl, int max_treelet_bytes, uint64_t blob_bytes, const rt_hit* hits,
+                       const uint32_t* visits, uint32_t n, uint32_t capacity, const rt_unit_config* cfg,
+                       rt_unit_stats* stats, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,7 @@
 #include "capi_internal.h"
 #include "trace_kernels.cuh"
 #include "prefetch_kernels.cuh"
+#include "replay_kernel.cuh"
 #include "trace_treelet.cuh"
 #include "treelets.h"
 
@@ -106,6 +107,7 @@ struct rt_scene {
   uint32_t* d_roots = nullptr;
   unsigned long long* d_member_first = nullptr;
   uint16_t* d_member_bytes = nullptr;
+  uint32_t* d_members = nullptr;
   uint32_t* d_hint = nullptr;  // staged-mode predictions (8 per treelet) or null
   uint32_t slot_bytes = 0;
   std::vector<uint16_t> route;  // routing bits of the treelet-ordered walk
@@ -158,6 +160,8 @@ void free_treelets(rt_scene* s) {
   cudaFree(s->d_roots);
   cudaFree(s->d_member_first);
   cudaFree(s->d_member_bytes);
+  cudaFree(s->d_members);
+  s->d_members = nullptr;
   cudaFree(s->d_hint);
   cudaFree(s->d_route);
   cudaFree(s->d_pin);
@@ -474,6 +478,13 @@ rt_status rt_treelets_form(rt_scene* s, uint32_t max_treelet_bytes, rt_treelet_i
   if (!p.member_bytes.empty())
     RT_CUDA(cudaMemcpy(s->d_member_bytes, p.member_bytes.data(), sizeof(uint16_t) * p.member_bytes.size(),
                        cudaMemcpyHostToDevice));
+  st = dalloc(&s->d_members, sizeof(uint32_t) * p.members.size());
+  if (st != RT_OK) {
+    free_treelets(s);
+    return st;
+  }
+  if (!p.members.empty())
+    RT_CUDA(cudaMemcpy(s->d_members, p.members.data(), sizeof(uint32_t) * p.members.size(), cudaMemcpyHostToDevice));
   s->slot_bytes = (p.largest_image + 127u) & ~127u;
   s->part = std::move(p);
   rtt::route_masks(s->host_blob.data(), s->blob_bytes, s->part, s->route);
@@ -739,6 +750,105 @@ extern "C" rt_status rt_prefetch_decide(rt_scene* s, const uint32_t* next_unit, 
   a.n_treelets = (uint32_t)s->part.roots.size();
   rtk::prefetch_decide_kernel<<<n_units, 512, 0, (cudaStream_t)stream>>>(a);
   RT_CUDA(cudaGetLastError());
+  return RT_OK;
+}
+
+extern "C" rt_status rt_unit_replay(rt_scene* s, const rt_hit* hits, const uint32_t* visits, uint32_t n,
+                                    uint32_t capacity, const rt_unit_config* cfg, rt_unit_stats* stats,
+                                    void* stream) {
+  if (!s || !cfg || !stats) return rti::fail(RT_ERR_INVALID, "rt_unit_replay: NULL argument");
+  if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_unit_replay: call rt_treelets_form first");
+  const rt_unit_config& c = *cfg;
+  auto bad = [](const char* m) { return rti::fail(RT_ERR_INVALID, std::string("rt_unit_replay: ") + m); };
+  if (c.n_rt_units == 0) return bad("n_rt_units must be >= 1");
+  if (c.max_warps == 0 || c.max_warps > rtr::kMaxResident) return bad("max_warps must be 1..16");
+  if (c.l1_sets == 0 || (c.l1_sets & (c.l1_sets - 1)) || c.l1_sets > 65536) return bad("l1_sets must be a power of two <= 65536");
+  if (c.l1_ways == 0 || c.l1_ways > 32) return bad("l1_ways must be 1..32");
+  if (c.hit_latency == 0 || c.miss_latency == 0 || c.miss_latency >= rtr::kMetaRing || c.hit_latency > c.miss_latency)
+    return bad("latencies must satisfy 1 <= hit <= miss < 4096");
+  if (c.prefetcher > RT_UNIT_PF_STRIDE || c.scheduler > RT_UNIT_SCHED_PMR) return bad("unknown prefetcher or scheduler");
+  if (c.prefetch_delay == 0) return bad("prefetch_delay must be >= 1");
+  if (c.decision.heuristic > RT_PREFETCH_LATTER) return bad("unknown heuristic");
+  if (n == 0) {
+    RT_CUDA(cudaMemsetAsync(stats, 0, sizeof(rt_unit_stats) * c.n_rt_units, (cudaStream_t)stream));
+    return RT_OK;
+  }
+  if (!hits || !visits || capacity == 0) return bad("hits and visits are required");
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  const uint64_t n_treelets = s->part.roots.size();
+  const uint64_t meta_size = (uint64_t)(s->part.max_bytes / 64) * 4;
+  const uint64_t meta_base = (s->blob_bytes + 4095) & ~4095ull;
+  // per-unit tables, sized to the sectors the unit can prefetch (blob and metadata), at most 2^20 entries
+  auto log2_ceil = [](uint64_t v) {
+    uint32_t l = 0;
+    while ((1ull << l) < v) ++l;
+    return l;
+  };
+  const uint64_t sectors = s->blob_bytes / 32 + n_treelets * meta_size / 32 + 4096;
+  const uint32_t tab_log2 = std::max<uint32_t>(12, std::min<uint32_t>(20, log2_ceil(2 * sectors)));
+  const uint32_t pq_cap = 1u << 18;
+  auto align = [](uint64_t v) { return (v + 255) & ~255ull; };
+  rtr::ReplayArgs a{};
+  uint64_t off = 0;
+  a.off_lines = off;
+  off = align(off + sizeof(rtr::Line) * (uint64_t)c.l1_sets * c.l1_ways);
+  a.off_sec = off;
+  off = align(off + sizeof(rtr::SectorEntry) * (1ull << tab_log2));
+  a.off_queued = off;
+  off = align(off + sizeof(rtr::QueuedEntry) * (1ull << tab_log2));
+  a.off_pq = off;
+  off = align(off + 16ull * pq_cap);
+  a.off_dead = off;
+  off = align(off + pq_cap);
+  a.off_chunk = off;
+  off = align(off + sizeof(rtr::Request) * rtr::kChunkCap);
+  a.off_warps = off;
+  off = align(off + sizeof(rtr::WarpSlot) * rtr::kMaxResident);
+  a.off_stride = off;
+  off = align(off + sizeof(rtr::StrideTable) * rtr::kMaxResident);
+  a.off_meta = off;
+  off = align(off + sizeof(rtr::MetaReturn) * rtr::kMetaRing);
+  a.off_keys = off;
+  off = align(off + sizeof(uint32_t) * 32 * rtr::kMaxResident);
+  a.unit_bytes = off;
+  const uint64_t total = off * c.n_rt_units;
+  uint8_t* scratch = nullptr;
+  rt_status st = dalloc(&scratch, total);
+  if (st != RT_OK) return st;
+  // the model's own bound on a unit's cycles: every round sends at most 128
+  // requests, then waits at most a miss latency plus an intersection latency
+  const uint64_t warps_per_unit = ((uint64_t)(n + 31) / 32 + c.n_rt_units - 1) / c.n_rt_units;
+  uint64_t cap = warps_per_unit * capacity * (rtr::kChunkCap + c.miss_latency + 8) + 1024;
+  if (c.max_cycles) cap = std::min<uint64_t>(cap, c.max_cycles);
+  a.cycle_cap = (uint32_t)std::min<uint64_t>(cap, rtr::kTimeCap);
+  a.hits = hits;
+  a.visits = visits;
+  a.n = n;
+  a.capacity = capacity;
+  a.cfg = c;
+  a.stats = stats;
+  a.meta = s->d_meta;
+  a.n_units = s->n_units;
+  a.roots = s->d_roots;
+  a.member_first = s->d_member_first;
+  a.members = s->d_members;
+  a.member_bytes = s->d_member_bytes;
+  a.n_treelets = (uint32_t)n_treelets;
+  a.meta_base = meta_base;
+  a.meta_size = meta_size;
+  a.scratch = scratch;
+  a.sec_log2 = a.queued_log2 = tab_log2;
+  a.pq_cap = pq_cap;
+  cudaStream_t sm = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, total, sm);
+  if (e == cudaSuccess) {
+    rtr::unit_replay_kernel<<<(c.n_rt_units + 63) / 64, 64, 0, sm>>>(a);
+    e = cudaGetLastError();
+  }
+  // the scratch is released once the replay has finished on the stream
+  if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
+  cudaFree(scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_unit_replay");
   return RT_OK;
 }
 

@@ -17,7 +17,9 @@ from ._ffi import (HIT_DTYPE, MODE_PLAIN, MODE_STAGED, MODE_TREELET, NO_TREELET,
                    RAY_FLAG_SKIP_CLOSEST_HIT, RAY_FLAG_TERMINATE_ON_FIRST_HIT, RAY_HIT_PROCEDURAL,
                    RAY_STACK_OVERFLOW, RAY_TRACE_OVERFLOW, SCENE_BLOBS, SCENE_CUBE, SCENE_CUBE_PLANE,
                    SCENE_SHARED_BLAS, SCENE_TERRAIN_INSTANCES, TX_BYTES, TX_NAMES, Camera, PrefetchParams,
-                   TUNING_OFF, PinnedInfo, RTError, TraceBuf, TraceStats, TreeletInfo, Tuning, check, lib, ptr)
+                   TUNING_OFF, PF_CLASSES, UNIT_PF_NONE, UNIT_PF_STRIDE, UNIT_PF_TREELET, UNIT_SCHED_FIRST,
+                   UNIT_SCHED_OMR, UNIT_SCHED_PMR, UNIT_STATS_DTYPE, PinnedInfo, RTError, TraceBuf, TraceStats,
+                   TreeletInfo, Tuning, UnitConfig, check, lib, ptr, unit_config)
 
 __all__ = [
     "Blob", "Context", "Scene", "camera_rays", "default_camera", "bounce_rays_host", "RTError", "lib",
@@ -322,6 +324,12 @@ class Scene:
                         stream: int = 0) -> None:
         check(lib().rt_prefetch_decide(self._h, ptr(next_unit), n_units, lanes, C.byref(params), ptr(state), ptr(out),
                                        C.c_void_p(stream)))
+
+    def unit_replay(self, hits, visits, n: int, capacity: int, config: UnitConfig, stats, stream: int = 0) -> None:
+        """RT-unit replay of a traced batch (device hits / visits / stats buffers;
+        stats holds config.n_rt_units records of UNIT_STATS_DTYPE)."""
+        check(lib().rt_unit_replay(self._h, ptr(hits), ptr(visits), n, capacity, C.byref(config), ptr(stats),
+                                   C.c_void_p(stream)))
 
 
 class Batch:

@@ -73,6 +73,37 @@ class PrefetchParams(C.Structure):
                 ("second_prefetch", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+UNIT_PF_NONE, UNIT_PF_TREELET, UNIT_PF_STRIDE = 0, 1, 2
+UNIT_SCHED_FIRST, UNIT_SCHED_OMR, UNIT_SCHED_PMR = 0, 1, 2
+PF_CLASSES = ("too_late", "late", "timely", "too_early", "never_used")
+
+
+class UnitConfig(C.Structure):
+    _fields_ = [("n_rt_units", C.c_uint32), ("max_warps", C.c_uint32), ("l1_sets", C.c_uint32),
+                ("l1_ways", C.c_uint32), ("hit_latency", C.c_uint32), ("miss_latency", C.c_uint32),
+                ("prefetcher", C.c_uint32), ("scheduler", C.c_uint32), ("decision", PrefetchParams),
+                ("prefetch_delay", C.c_uint32), ("load_metadata", C.c_uint32), ("wait_metadata", C.c_uint32),
+                ("max_cycles", C.c_uint32)]
+
+
+UNIT_STATS_DTYPE = np.dtype([(k, "<u8") for k in (
+    "cycles", "warps", "transactions", "demand_requests", "demand_hits", "demand_hit_reserved", "demand_misses",
+    "prefetch_queued", "prefetch_issued", "prefetch_removed", "prefetch_present", "prefetch_merged",
+    "prefetch_filled", "decisions", "treelets_prefetched", "metadata_queued")] +
+    [("effectiveness", "<u8", 5), ("unclassified_but_accessed", "<u8"), ("status", "<u8")])
+
+
+def unit_config(n_rt_units=16, max_warps=16, l1_sets=32, l1_ways=16, hit_latency=20, miss_latency=300,
+                prefetcher=UNIT_PF_NONE, scheduler=UNIT_SCHED_FIRST, heuristic=0, max_queue=1000000,
+                threshold=0.75, second_prefetch=0, prefetch_delay=1, load_metadata=0, wait_metadata=0,
+                max_cycles=0) -> UnitConfig:
+    """RT-unit replay settings; the defaults follow the reference's treelet
+    prefetching configuration (16 warps, a 32-set 16-way 128 B-line L1, delay 1)."""
+    return UnitConfig(n_rt_units, max_warps, l1_sets, l1_ways, hit_latency, miss_latency, prefetcher, scheduler,
+                      PrefetchParams(heuristic, max_queue, threshold, second_prefetch, 0), prefetch_delay,
+                      load_metadata, wait_metadata, max_cycles)
+
+
 PREFETCH_STATE_DTYPE = np.dtype([("last_prefetched", "<u4"), ("last_prefetched_second", "<u4"),
                                  ("last_rejected", "<u4"), ("queue_len", "<u4")])
 PREFETCH_DECISION_DTYPE = np.dtype([("treelet", "<u4"), ("count", "<u4"), ("total", "<u4"), ("submitted", "<u4"),
@@ -115,6 +146,7 @@ PROTOTYPES = {
     "rt_partition_route": (C.c_int, [vp, vp, vp]),
     "rt_partition_pinned": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, vp, u64p, C.POINTER(C.c_uint32)]),
     "rt_scene_set_pin_order": (C.c_int, [vp, vp, C.c_uint32]),
+    "rt_unit_replay": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.POINTER(UnitConfig), vp, vp]),
     "rt_scene_pinned_info": (C.c_int, [vp, C.POINTER(PinnedInfo)]),
     "rt_trace_host_noalloc": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
     "rt_batch_create": (C.c_int, [vp, C.POINTER(vp), C.c_uint32, C.POINTER(vp)]),
