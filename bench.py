@@ -655,14 +655,18 @@ def run_replay(args) -> None:
     torch.cuda.synchronize()
     setup = time.time() - t0
     base = dict(n_rt_units=args.rt_units, max_warps=16, l1_sets=32, l1_ways=16, hit_latency=20, miss_latency=300)
+    # treelet prefetchers with a prefetch queue of at most 4096 requests
+    # (-max_prefetch_queue_size); the stride prefetcher queues only while the
+    # queue holds at least that many entries, so it runs with 0
+    q = args.replay_queue
     variants = {
         "none": dict(),
-        "treelet_always": dict(prefetcher=1, heuristic=0),
-        "treelet_popularity_0.75": dict(prefetcher=1, heuristic=1, threshold=0.75),
-        "treelet_always_omr": dict(prefetcher=1, heuristic=0, scheduler=1),
-        "treelet_always_pmr": dict(prefetcher=1, heuristic=0, scheduler=2),
-        "treelet_always_metadata": dict(prefetcher=1, heuristic=0, load_metadata=1),
-        "treelet_always_metadata_wait": dict(prefetcher=1, heuristic=0, load_metadata=1, wait_metadata=1),
+        "treelet_always": dict(prefetcher=1, heuristic=0, max_queue=q),
+        "treelet_popularity_0.75": dict(prefetcher=1, heuristic=1, threshold=0.75, max_queue=q),
+        "treelet_always_omr": dict(prefetcher=1, heuristic=0, scheduler=1, max_queue=q),
+        "treelet_always_pmr": dict(prefetcher=1, heuristic=0, scheduler=2, max_queue=q),
+        "treelet_always_metadata": dict(prefetcher=1, heuristic=0, load_metadata=1, max_queue=q),
+        "treelet_always_metadata_wait": dict(prefetcher=1, heuristic=0, load_metadata=1, wait_metadata=1, max_queue=q),
         "stride_lee": dict(prefetcher=2, max_queue=0),
     }
     d_stats = torch.zeros(args.rt_units * rt.UNIT_STATS_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
@@ -685,6 +689,7 @@ def run_replay(args) -> None:
             "effectiveness": {c: round(float(eff[i] / max(1, pf)), 4) for i, c in enumerate(rt.PF_CLASSES)},
             "unclassified_but_accessed": round(float(s["unclassified_but_accessed"].sum() / max(1, pf)), 4),
             "status": int(np.bitwise_or.reduce(s["status"])), "replay_s_gpu": round(gpu_s[name], 3)}
+        print(f"replay {name}: {table[name]}", file=sys.stderr, flush=True)
     none_cycles = table["none"]["cycles"]
     for row in table.values():
         row["speedup_vs_none"] = round(none_cycles / max(1, row["cycles"]), 4)
@@ -737,7 +742,8 @@ def main():
                          "learned: the learned prefetcher against the heuristic; replay: RT-unit trace replay")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--train-steps", type=int, default=6000)
-    ap.add_argument("--replay-rays", type=int, default=65536)
+    ap.add_argument("--replay-rays", type=int, default=16384)
+    ap.add_argument("--replay-queue", type=int, default=4096)
     ap.add_argument("--rt-units", type=int, default=32)
     args = ap.parse_args()
     if args.workload == "replay" and args.impl != "reference":

@@ -18,6 +18,7 @@
 #include <map>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 namespace {
@@ -1160,6 +1161,7 @@ struct UnitReplay {
   std::vector<PrefetchRecord> records;
   std::map<uint64_t, int64_t> last_evicted;  // sector -> most recently evicted prefetch record
   std::deque<std::pair<uint64_t, uint64_t>> pq;  // prefetch_mem_access_q: (request, base)
+  std::unordered_map<uint64_t, uint32_t> queued;  // live copies of each address in pq
   std::deque<Request> chunk_q;                 // mem_access_q of the warp being served
   UnitWarp* serving = nullptr;
   std::list<UnitWarp> resident;                // m_current_warps, oldest first
@@ -1266,29 +1268,36 @@ struct UnitReplay {
 
   // Removes queued prefetches of this address, stepping past the entry that
   // follows each erased one (shader.cc:4657-4668 as written).
+  // (An address with no queued copy erases nothing, so the loop is skipped
+  // for it: `queued` counts the live copies of each address.)
   void remove_queued(uint64_t addr) {
+    auto q = queued.find(addr);
+    if (q == queued.end() || q->second == 0) return;
     for (size_t idx = 0; idx < pq.size(); idx++) {
       if (addr == pq[idx].first) {
         pq.erase(pq.begin() + (long)idx);
+        q->second--;
         st.prefetch_removed++;
       }
     }
+  }
+
+  void enqueue(uint64_t addr, uint64_t base) {
+    pq.emplace_back(addr, base);
+    queued[addr]++;
+    st.prefetch_queued++;
   }
 
   void push_member(const StackEntry& m, bool with_metadata) {
     if (with_metadata && cfg.load_metadata) {
       const uint64_t ma = meta_base + (uint64_t)metadata_idx[m.addr] * meta_size;
       for (uint64_t i = 0; i < meta_size / 32; ++i) {
-        pq.emplace_back(ma + i * 32, ma);
+        enqueue(ma + i * 32, ma);
         st.metadata_queued++;
-        st.prefetch_queued++;
       }
     }
     const uint64_t a = (uint64_t)(m.addr - tl->base);
-    for (int i = 0; i < (m.size + 31) / 32; ++i) {
-      pq.emplace_back(a + 32ull * i, a);
-      st.prefetch_queued++;
-    }
+    for (int i = 0; i < (m.size + 31) / 32; ++i) enqueue(a + 32ull * i, a);
   }
 
   // Lee MICRO'10 (shader.cc:4792-4826 as written: the last address is only
@@ -1308,12 +1317,8 @@ struct UnitReplay {
         largest_count = kv.second;
       }
     const uint64_t pa = next_addr + (uint64_t)(int64_t)largest_stride;
-    if (cfg.decision.max_queue <= pq.size()) {
-      for (unsigned i = 0; i < 2; ++i) {
-        pq.emplace_back(pa + i * 32, pa);
-        st.prefetch_queued++;
-      }
-    }
+    if (cfg.decision.max_queue <= pq.size())
+      for (unsigned i = 0; i < 2; ++i) enqueue(pa + i * 32, pa);
   }
 
   void decide() {
@@ -1470,6 +1475,7 @@ struct UnitReplay {
       } else if (cfg.prefetcher != RT_UNIT_PF_NONE && !pq.empty() && prefetch_issuable()) {
         const auto req = pq.front();
         pq.pop_front();
+        queued[req.first]--;
         prefetch(req.first, req.second, t);
       }
     }

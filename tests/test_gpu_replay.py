@@ -51,8 +51,8 @@ CONFIGS = [
     dict(prefetcher=1, heuristic=2, second_prefetch=1),
     dict(prefetcher=1, heuristic=3, scheduler=1, prefetch_delay=3),
     dict(prefetcher=1, heuristic=0, scheduler=2),
-    dict(prefetcher=1, heuristic=0, load_metadata=1),
-    dict(prefetcher=1, heuristic=0, load_metadata=1, wait_metadata=1),
+    dict(prefetcher=1, heuristic=0, load_metadata=1, max_queue=2048),
+    dict(prefetcher=1, heuristic=0, load_metadata=1, wait_metadata=1, max_queue=2048),
     dict(prefetcher=2, max_queue=0),
     dict(prefetcher=1, heuristic=0, max_queue=64),
 ]

@@ -317,15 +317,15 @@ struct PlainWalker {
     rec.rec(unit, rtf::TX_INTERNAL);
     rtd::Node64 nd;
     rtd::load64(v.blob + (uint64_t)unit * 4, 0, nd);
-    rtd::ChildHits ch;
-    if (inblas) {
-      const float cull = min_thit * ic.mult;
-      ch = ic_fast ? rtd::test_children<true>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull)
-                   : rtd::test_children<false>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull);
-    } else {
-      ch = fast ? rtd::test_children<true>(nd, unit, O, idir, tmin, tmax, min_thit)
-                : rtd::test_children<false>(nd, unit, O, idir, tmin, tmax, min_thit);
-    }
+    // one box test for both levels (the world ray, or the instance's object
+    // ray with the culling distance scaled into object space): lanes at TLAS
+    // and BLAS nodes run it together
+    const bool f = inblas ? ic_fast : fast;
+    const rtm::V3 o = inblas ? ic.o : O, id = inblas ? ic.idir : idir;
+    const float t0 = inblas ? ic.tmin : tmin, t1 = inblas ? ic.tmax : tmax;
+    const float cull = inblas ? min_thit * ic.mult : min_thit;
+    const rtd::ChildHits ch = f ? rtd::test_children<true>(nd, unit, o, id, t0, t1, cull)
+                                : rtd::test_children<false>(nd, unit, o, id, t0, t1, cull);
     const uint32_t level = inblas ? 0u : kTop;
     uint32_t c = ch.child_unit, nn = kNone;
 #pragma unroll

@@ -46,6 +46,10 @@ struct Walker {
   bool terminate, fast, ic_fast;  // FAST min/max allowed for the world / object ray
   uint32_t c_leaf, c_inst, status;
   EStack<CAP> cu, ot;
+  // The top of `cu` when it was pushed by the previous node visit: the node
+  // the walk pops next, kept in a register instead of a local-memory round
+  // trip (0 = none; no stack entry is 0, a blob's unit 0 is its TLAS header).
+  unsigned long long nxt;
   InstCtx ic;
   Recorder rec;
   SceneView v;
@@ -53,13 +57,19 @@ struct Walker {
   uint32_t pin_base;  // shared address of the pinned records, 0 = none
   uint32_t pin_root;  // record of the TLAS root node, 0 = not pinned
 
-  __device__ __forceinline__ bool active() const { return cu.n > 0 || ot.n > 0; }
+  __device__ __forceinline__ bool active() const { return nxt != 0 || cu.n > 0 || ot.n > 0; }
+
+  __device__ __forceinline__ void clear() {
+    nxt = 0;
+    cu.n = ot.n = 0;
+  }
 
   // Staged location (dense treelet << 10 | slot) of the node the ray visits
   // next, i.e. its first pending access; kNone for a pinned node.
   __device__ __forceinline__ uint32_t next_loc() const {
     unsigned long long e;
-    if (cu.n > 0) e = cu.top();
+    if (nxt) e = nxt;
+    else if (cu.n > 0) e = cu.top();
     else if (ot.n > 0) e = ot.top();
     else return kNone;
     if ((uint32_t)e & kEPin) return kNone;
@@ -69,12 +79,17 @@ struct Walker {
 
   __device__ __forceinline__ void push(bool same, uint32_t code, uint32_t inst) {
     const unsigned long long e = (unsigned long long)code | ((unsigned long long)inst << 32);
-    if (!(same ? cu.push(e) : ot.push(e))) status |= RT_RAY_STACK_OVERFLOW;
+    if (same) {
+      if (nxt && !cu.push(nxt)) status |= RT_RAY_STACK_OVERFLOW;
+      nxt = e;
+    } else if (!ot.push(e)) {
+      status |= RT_RAY_STACK_OVERFLOW;
+    }
   }
 
   __device__ __forceinline__ void bad_node() {
     status |= RT_RAY_BAD_NODE;
-    cu.n = ot.n = 0;
+    clear();
   }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
@@ -85,7 +100,7 @@ struct Walker {
     rec = Recorder{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
                    a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, v.meta};
     status = 0;
-    cu.n = ot.n = 0;
+    clear();
     min_thit = tmax;
     c_leaf = c_inst = 0;
     c_tobj = 0.0f;
@@ -121,8 +136,9 @@ struct Walker {
   // of a node staged in a warp slot, else 0.
   template <class Lookup>
   __device__ __forceinline__ void step(const TraceArgs& a, Lookup&& lookup) {
-    const bool from_cu = cu.n > 0;  // :1748-1754
-    const unsigned long long e = from_cu ? cu.pop() : ot.pop();
+    const bool from_cu = nxt != 0 || cu.n > 0;  // :1748-1754
+    const unsigned long long e = nxt ? nxt : (from_cu ? cu.pop() : ot.pop());
+    nxt = 0;
     const uint32_t code = (uint32_t)e, inst = (uint32_t)(e >> 32);
     const bool top = code & kTop, leaf = code & kLeaf, pinned = STAGED && (code & kEPin);
     const uint32_t rsh = from_cu ? 0u : 1u;  // which route bit applies
@@ -155,16 +171,14 @@ struct Walker {
       } else {
         rbits = __ldg(v.route + unit);
       }
-      rtd::ChildHits ch;
-      if (top) {
-        ch = fast ? rtd::test_children<true>(nd, unit, O, idir, tmin, tmax, min_thit)
-                  : rtd::test_children<false>(nd, unit, O, idir, tmin, tmax, min_thit);
-      } else {
-        ensure_instance(a, inst);
-        const float cull = min_thit * ic.mult;
-        ch = ic_fast ? rtd::test_children<true>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull)
-                     : rtd::test_children<false>(nd, unit, ic.o, ic.idir, ic.tmin, ic.tmax, cull);
-      }
+      // one box test for both levels, so lanes at TLAS and BLAS nodes run it together
+      if (!top) ensure_instance(a, inst);
+      const bool f = top ? fast : ic_fast;
+      const rtm::V3 o = top ? O : ic.o, id = top ? idir : ic.idir;
+      const float t0 = top ? tmin : ic.tmin, t1 = top ? tmax : ic.tmax;
+      const float cull = top ? min_thit : min_thit * ic.mult;
+      const rtd::ChildHits ch = f ? rtd::test_children<true>(nd, unit, o, id, t0, t1, cull)
+                                  : rtd::test_children<false>(nd, unit, o, id, t0, t1, cull);
       const uint32_t hit = ch.hit_mask;
       const uint64_t info = ch.info;
       const uint32_t same = rbits >> (rsh * kRouteOther);
@@ -236,7 +250,7 @@ struct Walker {
           c_leaf = unit;
           c_inst = inst;
           rec.rec(unit, rtf::TX_QUAD_LEAF_HIT);
-          if (terminate) cu.n = ot.n = 0;
+          if (terminate) clear();
         } else {
           rec.rec(unit, rtf::TX_QUAD_LEAF);
         }
@@ -245,7 +259,7 @@ struct Walker {
         rec.rec(unit, rtf::TX_PROCEDURAL_LEAF);
       }
     }
-    if (status & RT_RAY_STACK_OVERFLOW) cu.n = ot.n = 0;
+    if (status & RT_RAY_STACK_OVERFLOW) clear();
   }
 
   __device__ __forceinline__ void step(const TraceArgs& a) {
