@@ -790,8 +790,11 @@ extern "C" rt_status rt_unit_replay(rt_scene* s, const rt_hit* hits, const uint3
   auto align = [](uint64_t v) { return (v + 255) & ~255ull; };
   rtr::ReplayArgs a{};
   uint64_t off = 0;
+  // the L1 lines live in shared memory when they fit, else in the scratch slice
+  const uint64_t n_lines = (uint64_t)c.l1_sets * c.l1_ways;
+  a.lines_shared = n_lines <= rtr::kSmemLinesMax ? 1u : 0u;
   a.off_lines = off;
-  off = align(off + sizeof(rtr::Line) * (uint64_t)c.l1_sets * c.l1_ways);
+  if (!a.lines_shared) off = align(off + sizeof(rtr::Line) * n_lines);
   a.off_sec = off;
   off = align(off + sizeof(rtr::SectorEntry) * (1ull << tab_log2));
   a.off_queued = off;
@@ -800,16 +803,8 @@ extern "C" rt_status rt_unit_replay(rt_scene* s, const rt_hit* hits, const uint3
   off = align(off + 16ull * pq_cap);
   a.off_dead = off;
   off = align(off + pq_cap);
-  a.off_chunk = off;
-  off = align(off + sizeof(rtr::Request) * rtr::kChunkCap);
-  a.off_warps = off;
-  off = align(off + sizeof(rtr::WarpSlot) * rtr::kMaxResident);
-  a.off_stride = off;
-  off = align(off + sizeof(rtr::StrideTable) * rtr::kMaxResident);
   a.off_meta = off;
   off = align(off + sizeof(rtr::MetaReturn) * rtr::kMetaRing);
-  a.off_keys = off;
-  off = align(off + sizeof(uint32_t) * 32 * rtr::kMaxResident);
   a.unit_bytes = off;
   const uint64_t total = off * c.n_rt_units;
   uint8_t* scratch = nullptr;
@@ -842,8 +837,13 @@ extern "C" rt_status rt_unit_replay(rt_scene* s, const rt_hit* hits, const uint3
   cudaStream_t sm = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(scratch, 0, total, sm);
   if (e == cudaSuccess) {
-    rtr::unit_replay_kernel<<<(c.n_rt_units + 63) / 64, 64, 0, sm>>>(a);
-    e = cudaGetLastError();
+    // one warp (CTA) per RT unit, its state in shared memory
+    const size_t smem = ((sizeof(rtr::UnitShared) + 15) & ~(size_t)15) + (a.lines_shared ? sizeof(rtr::Line) * n_lines : 0);
+    e = cudaFuncSetAttribute(rtr::unit_replay_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+      rtr::unit_replay_kernel<<<c.n_rt_units, 32, smem, sm>>>(a);
+      e = cudaGetLastError();
+    }
   }
   // the scratch is released once the replay has finished on the stream
   if (e == cudaSuccess) e = cudaStreamSynchronize(sm);

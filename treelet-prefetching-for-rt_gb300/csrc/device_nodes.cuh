@@ -141,6 +141,19 @@ struct Instance {
   uint32_t instance_id;
 };
 
+// The same fields when the leaf's first 64 bytes are already loaded in q:
+// two more 16-byte loads (bytes 64..79 and 112..127).
+__device__ __forceinline__ void instance_from(const Node64& q, const uint4* g, uint32_t saddr, Instance& in) {
+  const uint4 d = load16(g, saddr, 4), e = load16(g, saddr, 7);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) in.w2o.m[k / 3][k % 3] = __uint_as_float(q.w[4 + k]);
+  in.w2o.m[3][0] = __uint_as_float(e.y);
+  in.w2o.m[3][1] = __uint_as_float(e.z);
+  in.w2o.m[3][2] = __uint_as_float(e.w);
+  in.bvh_address = (uint64_t)d.x | ((uint64_t)d.y << 32);
+  in.instance_id = d.z;
+}
+
 __device__ __forceinline__ void load_instance(const uint4* g, uint32_t saddr, Instance& in) {
   const uint4 a = load16(g, saddr, 1), b = load16(g, saddr, 2), c = load16(g, saddr, 3);
   const uint4 d = load16(g, saddr, 4), e = load16(g, saddr, 7);

@@ -312,11 +312,8 @@ struct PlainWalker {
     next = kNone;
   }
 
-  __device__ __forceinline__ void visit_internal(const TraceArgs& a, uint32_t unit) {
-    if (unit >= v.n_units) return stop(RT_RAY_BAD_NODE);
+  __device__ __forceinline__ void visit_internal(const TraceArgs& a, uint32_t unit, const rtd::Node64& nd) {
     rec.rec(unit, rtf::TX_INTERNAL);
-    rtd::Node64 nd;
-    rtd::load64(v.blob + (uint64_t)unit * 4, 0, nd);
     // one box test for both levels (the world ray, or the instance's object
     // ray with the culling distance scaled into object space): lanes at TLAS
     // and BLAS nodes run it together
@@ -342,11 +339,8 @@ struct PlainWalker {
     if (status & RT_RAY_STACK_OVERFLOW) stop(0);
   }
 
-  __device__ __forceinline__ void visit_leaf(const TraceArgs& a, uint32_t unit) {
-    if (unit >= v.n_units) return stop(RT_RAY_BAD_NODE);
+  __device__ __forceinline__ void visit_leaf(const TraceArgs& a, uint32_t unit, const rtd::Node64& q) {
     rec.rec(unit, rtf::TX_LEAF_DESC);
-    rtd::Node64 q;
-    rtd::load64(v.blob + (uint64_t)unit * 4, 0, q);
     if (rtf::leaf_type_of(q.w[1]) == 0) {
       const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
       const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
@@ -370,11 +364,10 @@ struct PlainWalker {
     }
   }
 
-  __device__ __forceinline__ void visit_instance(const TraceArgs& a, uint32_t unit) {
-    if (unit + 1 >= v.n_units) return stop(RT_RAY_BAD_NODE);
+  __device__ __forceinline__ void visit_instance(const TraceArgs& a, uint32_t unit, const rtd::Node64& q) {
     rec.rec(unit, rtf::TX_INSTANCE_LEAF);
     rtd::Instance in;
-    rtd::load_instance(v.blob + (uint64_t)unit * 4, 0, in);
+    rtd::instance_from(q, v.blob + (uint64_t)unit * 4, 0, in);
     const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
     if ((hdr & 63) || hdr / 64 >= v.n_units) return stop(RT_RAY_BAD_NODE);
     rec.rec((uint32_t)(hdr >> 6), rtf::TX_STRUCTURE);
@@ -387,14 +380,25 @@ struct PlainWalker {
     if (status & RT_RAY_STACK_OVERFLOW) stop(0);
   }
 
-  // One node visit (the caller checks active() first).
+  // One node visit (the caller checks active() first).  The node to visit is
+  // found first and its first 64 bytes loaded once for every kind, so a
+  // warp's lanes at internal nodes, leaves and instance leaves issue one load.
   __device__ __forceinline__ void step(const TraceArgs& a) {
+    uint32_t unit, kind;  // 0 internal node, 1 primitive leaf, 2 instance leaf
     for (;;) {
-      if (next != kNone) return visit_internal(a, next);
+      if (next != kNone) {
+        unit = next;
+        kind = 0;
+        break;
+      }
       if (inblas) {
         if (sp > 0 && !(stk[sp - 1] & kTop)) {
           const uint32_t e = pop();
-          if (e & kLeaf) return visit_leaf(a, e >> 2);
+          if (e & kLeaf) {
+            unit = e >> 2;
+            kind = 1;
+            break;
+          }
           next = e >> 2;
           continue;
         }
@@ -407,8 +411,16 @@ struct PlainWalker {
         next = e >> 2;
         continue;
       }
-      return visit_instance(a, e >> 2);
+      unit = e >> 2;
+      kind = 2;
+      break;
     }
+    if (unit + (kind == 2 ? 1u : 0u) >= v.n_units) return stop(RT_RAY_BAD_NODE);
+    rtd::Node64 q;
+    rtd::load64(v.blob + (uint64_t)unit * 4, 0, q);
+    if (kind == 0) visit_internal(a, unit, q);
+    else if (kind == 1) visit_leaf(a, unit, q);
+    else visit_instance(a, unit, q);
   }
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {

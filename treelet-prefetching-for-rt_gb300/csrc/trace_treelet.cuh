@@ -157,11 +157,13 @@ struct Walker {
       }
     }
     const uint4* g = v.blob + (uint64_t)unit * 4;
+    // the first 64 bytes (or the whole pinned record of an instance leaf), for
+    // every kind of node at once, so the warp's lanes issue one load
+    rtd::Node64 nd;
+    rtd::load64(g, saddr, nd);
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
       rec.rec(unit, rtf::TX_INTERNAL);
       uint32_t soff01 = 0, soff23 = 0, soff45 = 0;
-      rtd::Node64 nd;
-      rtd::load64(g, saddr, nd);
       if (pinned) {  // route bits in bytes 16..17, child records in the tail
         const uint4 t = rtd::ld_shared_v4(saddr + rtp::IN_UNIT);
         rbits = nd.w[rtp::IN_ROUTE / 4] & 0xffffu;
@@ -200,26 +202,16 @@ struct Walker {
       rec.rec(unit, rtf::TX_INSTANCE_LEAF);
       uint32_t hdr_unit, broot_unit, broot_soff = 0;
       rtd::Instance in;
-      if (pinned) {
-        const uint4 h = rtd::ld_shared_v4(saddr);
-        hdr_unit = h.y;
-        broot_unit = h.z;
-        rbits = h.w & 0xffffu;
-        broot_soff = h.w >> 16;
-        float m[12];
+      if (pinned) {  // the 64-byte record: units, route bits, BLAS root record, rows
+        hdr_unit = nd.w[rtp::IL_HDR_UNIT / 4];
+        broot_unit = nd.w[rtp::IL_BROOT_UNIT / 4];
+        rbits = nd.w[rtp::IL_ROUTE / 4] & 0xffffu;
+        broot_soff = nd.w[rtp::IL_ROUTE / 4] >> 16;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const uint4 q = rtd::ld_shared_v4(saddr + rtp::IL_W2O + 16u * k);
-          m[4 * k + 0] = __uint_as_float(q.x);
-          m[4 * k + 1] = __uint_as_float(q.y);
-          m[4 * k + 2] = __uint_as_float(q.z);
-          m[4 * k + 3] = __uint_as_float(q.w);
-        }
-#pragma unroll
-        for (int k = 0; k < 12; ++k) in.w2o.m[k / 3][k % 3] = m[k];
+        for (int k = 0; k < 12; ++k) in.w2o.m[k / 3][k % 3] = __uint_as_float(nd.w[rtp::IL_W2O / 4 + k]);
       } else {
         rbits = __ldg(v.route + unit);
-        rtd::load_instance(g, saddr, in);
+        rtd::instance_from(nd, g, saddr, in);
         const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
         if ((hdr & 63) || hdr / 64 >= v.n_units) return bad_node();
         hdr_unit = (uint32_t)(hdr >> 6);
@@ -234,8 +226,7 @@ struct Walker {
       push((rbits >> (kRouteInst + rsh)) & 1u, cc, unit);
     } else {  // primitive leaf (:2071-2196)
       rec.rec(unit, rtf::TX_LEAF_DESC);
-      rtd::Node64 q;
-      rtd::load64(g, saddr, q);
+      const rtd::Node64& q = nd;
       if (rtf::leaf_type_of(q.w[1]) == 0) {
         ensure_instance(a, inst);
         const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
