@@ -124,14 +124,6 @@ struct Walker {
     }
   }
 
-  __device__ __forceinline__ void ensure_instance(const TraceArgs& a, uint32_t inst) {
-    if (ic.unit == inst) return;
-    rtd::Instance in;
-    rtd::load_instance(v.blob + (uint64_t)inst * 4, 0, in);
-    enter_instance(in, inst, O, D, tmin, tmax, ic);
-    ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
-  }
-
   // Visits one node; `lookup(unit, meta)` returns the shared-memory address
   // of a node staged in a warp slot, else 0.
   template <class Lookup>
@@ -160,7 +152,44 @@ struct Walker {
     // the first 64 bytes (or the whole pinned record of an instance leaf), for
     // every kind of node at once, so the warp's lanes issue one load
     rtd::Node64 nd;
-    rtd::load64(g, saddr, nd);
+    if (STAGED) {
+      // one generic load for lanes reading shared memory and lanes reading
+      // global memory, instead of both load paths for a mixed warp
+      const uint4* src = saddr ? reinterpret_cast<const uint4*>(__cvta_shared_to_generic(saddr)) : g;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint4 w = src[k];
+        nd.w[4 * k + 0] = w.x;
+        nd.w[4 * k + 1] = w.y;
+        nd.w[4 * k + 2] = w.z;
+        nd.w[4 * k + 3] = w.w;
+      }
+    } else {
+      rtd::load64(g, 0, nd);
+    }
+    // The instance context, once for every kind of node: an instance leaf
+    // enters its own instance; a BLAS node needs its instance's object ray,
+    // recomputed when the walk comes back from another instance's nodes
+    // (make_transformed_ray is deterministic, so recomputing gives the
+    // reference's stored objectRay).  Lanes of all kinds switch together.
+    rtd::Instance in;
+    uint32_t enter = kNone;
+    if (top && leaf) {
+      if (pinned) {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) in.w2o.m[k / 3][k % 3] = __uint_as_float(nd.w[rtp::IL_W2O / 4 + k]);
+      } else {
+        rtd::instance_from(nd, g, saddr, in);
+      }
+      enter = unit;
+    } else if (!top && inst != ic.unit) {
+      rtd::load_instance(v.blob + (uint64_t)inst * 4, 0, in);
+      enter = inst;
+    }
+    if (enter != kNone) {
+      enter_instance(in, enter, O, D, tmin, tmax, ic);
+      ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
+    }
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
       rec.rec(unit, rtf::TX_INTERNAL);
       uint32_t soff01 = 0, soff23 = 0, soff45 = 0;
@@ -174,7 +203,6 @@ struct Walker {
         rbits = __ldg(v.route + unit);
       }
       // one box test for both levels, so lanes at TLAS and BLAS nodes run it together
-      if (!top) ensure_instance(a, inst);
       const bool f = top ? fast : ic_fast;
       const rtm::V3 o = top ? O : ic.o, id = top ? idir : ic.idir;
       const float t0 = top ? tmin : ic.tmin, t1 = top ? tmax : ic.tmax;
@@ -201,17 +229,13 @@ struct Walker {
     } else if (top) {  // instance leaf (:1870-1953)
       rec.rec(unit, rtf::TX_INSTANCE_LEAF);
       uint32_t hdr_unit, broot_unit, broot_soff = 0;
-      rtd::Instance in;
       if (pinned) {  // the 64-byte record: units, route bits, BLAS root record, rows
         hdr_unit = nd.w[rtp::IL_HDR_UNIT / 4];
         broot_unit = nd.w[rtp::IL_BROOT_UNIT / 4];
         rbits = nd.w[rtp::IL_ROUTE / 4] & 0xffffu;
         broot_soff = nd.w[rtp::IL_ROUTE / 4] >> 16;
-#pragma unroll
-        for (int k = 0; k < 12; ++k) in.w2o.m[k / 3][k % 3] = __uint_as_float(nd.w[rtp::IL_W2O / 4 + k]);
       } else {
         rbits = __ldg(v.route + unit);
-        rtd::instance_from(nd, g, saddr, in);
         const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
         if ((hdr & 63) || hdr / 64 >= v.n_units) return bad_node();
         hdr_unit = (uint32_t)(hdr >> 6);
@@ -220,15 +244,12 @@ struct Walker {
         broot_unit = (uint32_t)(broot >> 6);
       }
       rec.rec(hdr_unit, rtf::TX_STRUCTURE);
-      enter_instance(in, unit, O, D, tmin, tmax, ic);
-      ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
       const uint32_t cc = broot_soff ? ((broot_soff << kEShift) | kEPin) : (broot_unit << kEShift);
       push((rbits >> (kRouteInst + rsh)) & 1u, cc, unit);
     } else {  // primitive leaf (:2071-2196)
       rec.rec(unit, rtf::TX_LEAF_DESC);
       const rtd::Node64& q = nd;
       if (rtf::leaf_type_of(q.w[1]) == 0) {
-        ensure_instance(a, inst);
         const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
         const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
         const rtm::V3 v2 = rtm::v3(__uint_as_float(q.w[10]), __uint_as_float(q.w[11]), __uint_as_float(q.w[12]));
