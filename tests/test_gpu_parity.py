@@ -210,3 +210,44 @@ def test_staged_serves_from_shared_memory(ctx):
     assert st["stagings"] > 0 and st["staged_bytes"] > 0
     assert st["smem_reads"] > 0
     scene.close()
+
+
+@pytest.mark.parametrize("n", [525_288, 1_126_400])
+def test_host_trace_chunks_match_device_trace(ctx, n):
+    """rt_trace_host pipelines calls of 2^19 rays or more in chunks (copies of
+    one chunk overlap the trace of another): its hits, visit and treelet rows
+    and summed counters must equal one device-side rt_trace of the same rays."""
+    import torch
+
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 256 * 256, 3)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_TERRAIN_INSTANCES), 1024, 1100, 1, 4, 1e-4, 1e30)[:n]
+    rng = np.random.default_rng(n)
+    flags = rng.choice(np.array([rt.RAY_FLAG_OPAQUE, rt.RAY_FLAG_OPAQUE | rt.RAY_FLAG_TERMINATE_ON_FIRST_HIT, 0],
+                                np.uint32), size=n)
+    cap = 24 if n < 1_000_000 else 0
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    d_rays = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8)).cuda()
+    d_flags = torch.from_numpy(flags.view(np.uint8)).cuda()
+    for mode, _, name in _modes():
+        hits, vis, tids = scene.trace_host(rays, mode, flags=flags, capacity=cap, want_visits=cap > 0,
+                                           want_treelets=cap > 0)
+        host_stats = scene.stats()
+        d_hits = torch.zeros(n * 64, dtype=torch.uint8, device="cuda")
+        d_vis = torch.zeros(n * max(cap, 1), dtype=torch.int32, device="cuda") if cap else None
+        d_tl = torch.zeros(n * max(cap, 1), dtype=torch.int32, device="cuda") if cap else None
+        scene.trace(d_rays, d_hits, mode, flags=d_flags, visits=d_vis, treelets=d_tl, capacity=cap, n=n)
+        torch.cuda.synchronize()
+        dev_stats = scene.stats()
+        ref = d_hits.cpu().numpy().view(rt.HIT_DTYPE)
+        assert hits.tobytes() == ref.tobytes(), f"{name}: host-path hits differ from device-path hits"
+        if cap:  # entries past a ray's visit count are not written
+            assert_traces_equal(vis, d_vis.cpu().numpy().view(np.uint32).reshape(n, cap), ref["n_visits"],
+                                f"{name} visit rows")
+            assert_traces_equal(tids, d_tl.cpu().numpy().view(np.uint32).reshape(n, cap), ref["n_visits"],
+                                f"{name} treelet rows")
+        assert host_stats["node_bytes"] == dev_stats["node_bytes"] > 0, name
+        assert host_stats["device_status"] == dev_stats["device_status"] == 0, name
+    scene.close()

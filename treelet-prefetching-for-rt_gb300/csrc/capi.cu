@@ -123,8 +123,11 @@ struct rt_scene {
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
   rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096};
-  // host-buffer path scratch
-  cudaStream_t stream = nullptr;
+  // host-buffer path: a copy-in stream, two trace streams (chunk c on
+  // stream / stream2 by parity, so one chunk's launch fills the SMs that the
+  // previous chunk's last rays leave idle), a copy-out stream, and events
+  cudaStream_t stream = nullptr, stream2 = nullptr, xin = nullptr, xout = nullptr;
+  cudaEvent_t ev_in[rti::kHostChunks] = {}, ev_done[rti::kHostChunks] = {};
   void* d_io = nullptr;
   size_t io_bytes = 0;
 };
@@ -301,14 +304,17 @@ rt_status merge_tuning(const rt_tuning& cur, const rt_tuning* t, rt_tuning& n) {
   return RT_OK;
 }
 
-// Zeroes the launch's counters and queue, then launches the kernel of `mode`
-// with stack depth CAP.
+// Zeroes the launch's queue (and its counters unless `keep` is set: chunks of
+// one call add up), then launches the kernel of `mode` with stack depth CAP.
 template <int CAP>
-rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint32_t largest_image, cudaStream_t st) {
+rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint32_t largest_image, cudaStream_t st,
+                     bool keep) {
   a.epoch = t.staged_epoch;
   a.refill = t.refill_lanes;
-  RT_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, st));
-  RT_CUDA(cudaMemsetAsync(a.status, 0, sizeof(uint32_t), st));
+  if (!keep) {
+    RT_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, st));
+    RT_CUDA(cudaMemsetAsync(a.status, 0, sizeof(uint32_t), st));
+  }
   RT_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), st));
   if (mode == RT_MODE_PLAIN) {
     const uint32_t bt = t.block_threads;
@@ -347,14 +353,14 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
 // Stack depths compiled in (entries per stack per ray); a ray that needs more
 // is flagged RT_RAY_STACK_OVERFLOW.
 rt_status launch_trace(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint32_t largest_image,
-                       cudaStream_t st) {
+                       cudaStream_t st, bool keep = false) {
   switch (t.stack_depth) {
     case 48:
-      return launch_cap<48>(a, mode, t, largest_image, st);
+      return launch_cap<48>(a, mode, t, largest_image, st, keep);
     case 160:
-      return launch_cap<160>(a, mode, t, largest_image, st);
+      return launch_cap<160>(a, mode, t, largest_image, st, keep);
     default:
-      return launch_cap<96>(a, mode, t, largest_image, st);
+      return launch_cap<96>(a, mode, t, largest_image, st, keep);
   }
 }
 
@@ -407,7 +413,7 @@ rt_status rt_scene_create(rt_ctx* ctx, const rt_blob* blob, rt_scene** out) {
   rt_status st = dalloc(&s->d_blob, s->blob_bytes);
   if (st == RT_OK) st = dalloc(&s->d_stats, sizeof(unsigned long long) * rtk::ST_COUNT);
   if (st == RT_OK) st = dalloc(&s->d_status, sizeof(uint32_t));
-  if (st == RT_OK) st = dalloc(&s->d_queue, sizeof(uint32_t));
+  if (st == RT_OK) st = dalloc(&s->d_queue, sizeof(uint32_t) * rti::kHostChunks);
   if (st != RT_OK) {
     rt_scene_destroy(s);
     return st;
@@ -415,7 +421,12 @@ rt_status rt_scene_create(rt_ctx* ctx, const rt_blob* blob, rt_scene** out) {
   cudaError_t e = cudaMemcpy(s->d_blob, blob->bytes.data(), s->blob_bytes, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT);
   if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  for (cudaStream_t* x : {&s->stream, &s->stream2, &s->xin, &s->xout})
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(x, cudaStreamNonBlocking);
+  for (uint32_t c = 0; c < rti::kHostChunks; ++c) {
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_in[c], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_done[c], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     rt_scene_destroy(s);
     return cuda_fail(e, "rt_scene_create");
@@ -433,7 +444,12 @@ rt_status rt_scene_destroy(rt_scene* s) {
   cudaFree(s->d_status);
   cudaFree(s->d_queue);
   cudaFree(s->d_io);
-  if (s->stream) cudaStreamDestroy(s->stream);
+  for (uint32_t c = 0; c < rti::kHostChunks; ++c) {
+    if (s->ev_in[c]) cudaEventDestroy(s->ev_in[c]);
+    if (s->ev_done[c]) cudaEventDestroy(s->ev_done[c]);
+  }
+  for (cudaStream_t x : {s->stream, s->stream2, s->xin, s->xout})
+    if (x) cudaStreamDestroy(x);
   delete s;
   return RT_OK;
 }
@@ -570,21 +586,28 @@ rt_status rt_scene_get_tuning(const rt_scene* s, rt_tuning* t) {
   return RT_OK;
 }
 
-rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t n,
-                   uint32_t mode, rt_hit* hits, const rt_trace_buf* trace, void* stream) {
-  if (!s) return rti::fail(RT_ERR_INVALID, "rt_trace: NULL scene");
-  if (n == 0) return RT_OK;
-  if (!rays || !hits) return rti::fail(RT_ERR_INVALID, "rt_trace: NULL rays or hits");
-  if (mode > RT_MODE_STAGED) return rti::fail(RT_ERR_INVALID, "rt_trace: unknown mode");
+}  // extern "C"
+
+namespace {
+
+// Argument checks shared by rt_trace and rt_trace_host.
+rt_status check_trace(const rt_scene* s, uint32_t mode, const rt_trace_buf* trace, const char* who) {
+  if (mode > RT_MODE_STAGED) return rti::fail(RT_ERR_INVALID, std::string(who) + ": unknown mode");
   const bool want_tl = trace && trace->treelets;
   if ((mode != RT_MODE_PLAIN || want_tl) && !s->has_treelets)
-    return rti::fail(RT_ERR_STATE, "rt_trace: call rt_treelets_form first");
+    return rti::fail(RT_ERR_STATE, std::string(who) + ": call rt_treelets_form first");
   if (trace && (trace->visits || trace->treelets) && trace->capacity == 0)
-    return rti::fail(RT_ERR_INVALID, "rt_trace: trace capacity is 0");
+    return rti::fail(RT_ERR_INVALID, std::string(who) + ": trace capacity is 0");
   if (mode == RT_MODE_STAGED && s->part.roots.size() >= rtt::kMaxDense)
-    return rti::fail(RT_ERR_TOO_LARGE, "rt_trace: too many treelets for staged mode (max 4194304)");
-  cudaStream_t st = (cudaStream_t)stream;
-  RT_CUDA(cudaSetDevice(s->ctx->device));
+    return rti::fail(RT_ERR_TOO_LARGE, std::string(who) + ": too many treelets for staged mode (max 4194304)");
+  return RT_OK;
+}
+
+// Launches one trace over device arrays.  `queue` is the ray hand-out
+// counter of this launch; `keep` adds the counters to the previous launch's.
+rt_status trace_launch(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t n,
+                       uint32_t mode, rt_hit* hits, const rt_trace_buf* trace, cudaStream_t st, uint32_t* queue,
+                       bool keep) {
   rtk::TraceArgs a{};
   a.blob = reinterpret_cast<const uint4*>(s->d_blob);
   a.n_units = s->n_units;
@@ -608,9 +631,37 @@ rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint3
   a.n_treelets = s->has_treelets ? (uint32_t)s->part.roots.size() : 0;
   a.stats = s->d_stats;
   a.status = s->d_status;
-  a.queue = s->d_queue;
+  a.queue = queue;
   a.hint = s->d_hint;
-  return launch_trace(a, mode, s->tuning, s->slot_bytes, st);
+  return launch_trace(a, mode, s->tuning, s->slot_bytes, st, keep);
+}
+
+// Waits for every stream of the host path; returns `st` (or the first CUDA
+// error if `st` is RT_OK).
+rt_status host_finish(rt_scene* s, rt_status st) {
+  cudaError_t e = cudaSuccess;
+  for (cudaStream_t x : {s->xin, s->stream, s->stream2, s->xout}) {
+    if (!x) continue;
+    const cudaError_t ex = cudaStreamSynchronize(x);
+    if (e == cudaSuccess) e = ex;
+  }
+  if (st == RT_OK && e != cudaSuccess) return cuda_fail(e, "rt_trace_host");
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+rt_status rt_trace(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t n,
+                   uint32_t mode, rt_hit* hits, const rt_trace_buf* trace, void* stream) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_trace: NULL scene");
+  if (n == 0) return RT_OK;
+  if (!rays || !hits) return rti::fail(RT_ERR_INVALID, "rt_trace: NULL rays or hits");
+  rt_status st = check_trace(s, mode, trace, "rt_trace");
+  if (st != RT_OK) return st;
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  return trace_launch(s, rays, flags, default_flags, n, mode, hits, trace, (cudaStream_t)stream, s->d_queue, false);
 }
 
 rt_status rt_scene_set_stage_hints(rt_scene* s, const uint32_t* hints) {
@@ -647,6 +698,8 @@ rt_status rt_trace_host(rt_scene* s, const rt_ray* rays, const uint32_t* flags, 
   if (!s) return rti::fail(RT_ERR_INVALID, "rt_trace_host: NULL scene");
   if (n == 0) return RT_OK;
   if (!rays || !hits) return rti::fail(RT_ERR_INVALID, "rt_trace_host: NULL rays or hits");
+  rt_status st = check_trace(s, mode, trace, "rt_trace_host");
+  if (st != RT_OK) return st;
   RT_CUDA(cudaSetDevice(s->ctx->device));
   const uint32_t cap = (trace && (trace->visits || trace->treelets)) ? trace->capacity : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -659,7 +712,7 @@ rt_status rt_trace_host(rt_scene* s, const rt_ray* rays, const uint32_t* flags, 
     cudaFree(s->d_io);
     s->d_io = nullptr;
     s->io_bytes = 0;
-    rt_status st = dalloc((uint8_t**)&s->d_io, need);
+    st = dalloc((uint8_t**)&s->d_io, need);
     if (st != RT_OK) return st;
     s->io_bytes = need;
   }
@@ -669,19 +722,43 @@ rt_status rt_trace_host(rt_scene* s, const rt_ray* rays, const uint32_t* flags, 
   rt_hit* d_hits = (rt_hit*)(base + b_rays + b_flags);
   uint32_t* d_vis = b_vis ? (uint32_t*)(base + b_rays + b_flags + b_hits) : nullptr;
   uint32_t* d_tl = b_tl ? (uint32_t*)(base + b_rays + b_flags + b_hits + b_vis) : nullptr;
-  RT_CUDA(cudaMemcpyAsync(d_rays, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-  if (flags) RT_CUDA(cudaMemcpyAsync(d_flags, flags, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-  rt_trace_buf tb{d_vis, d_tl, cap};
-  rt_status st = rt_trace(s, d_rays, d_flags, default_flags, n, mode, d_hits, cap ? &tb : nullptr, s->stream);
-  if (st != RT_OK) return st;
-  RT_CUDA(cudaMemcpyAsync(hits, d_hits, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
-  if (d_vis)
-    RT_CUDA(cudaMemcpyAsync(trace->visits, d_vis, sizeof(uint32_t) * (size_t)n * cap, cudaMemcpyDeviceToHost, s->stream));
-  if (d_tl)
-    RT_CUDA(cudaMemcpyAsync(trace->treelets, d_tl, sizeof(uint32_t) * (size_t)n * cap, cudaMemcpyDeviceToHost,
-                            s->stream));
-  RT_CUDA(cudaStreamSynchronize(s->stream));
-  return RT_OK;
+
+  // Chunks pipeline the copies with the traces: rays of chunk c+1 go in and
+  // hits of chunk c-1 come out while chunk c is traced.
+  uint64_t bound[rti::kHostChunks + 1];
+  const uint32_t chunks = rti::host_chunk_bounds(n, bound);
+  // counters of the whole call start at zero, ahead of every chunk's copy-in
+  RT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, s->xin));
+  RT_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->xin));
+  cudaError_t e = cudaSuccess;
+  for (uint32_t c = 0; c < chunks && e == cudaSuccess && st == RT_OK; ++c) {
+    const size_t lo = bound[c], m = bound[c + 1] - bound[c];
+    e = cudaMemcpyAsync(d_rays + lo, rays + lo, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, s->xin);
+    if (e == cudaSuccess && flags)
+      e = cudaMemcpyAsync(d_flags + lo, flags + lo, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, s->xin);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev_in[c], s->xin);
+    cudaStream_t cs = (c & 1) ? s->stream2 : s->stream;
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, s->ev_in[c], 0);
+    if (e != cudaSuccess) break;
+    rt_trace_buf tb{d_vis ? d_vis + lo * cap : nullptr, d_tl ? d_tl + lo * cap : nullptr, cap};
+    st = trace_launch(s, d_rays + lo, d_flags ? d_flags + lo : nullptr, default_flags, (uint32_t)m, mode, d_hits + lo,
+                      cap ? &tb : nullptr, cs, s->d_queue + c, true);
+    if (st == RT_OK) e = cudaEventRecord(s->ev_done[c], cs);
+  }
+  for (uint32_t c = 0; c < chunks && e == cudaSuccess && st == RT_OK; ++c) {
+    const size_t lo = bound[c], m = bound[c + 1] - bound[c];
+    e = cudaStreamWaitEvent(s->xout, s->ev_done[c], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hits + lo, d_hits + lo, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, s->xout);
+    if (e == cudaSuccess && d_vis)
+      e = cudaMemcpyAsync(trace->visits + lo * cap, d_vis + lo * cap, sizeof(uint32_t) * m * cap,
+                          cudaMemcpyDeviceToHost, s->xout);
+    if (e == cudaSuccess && d_tl)
+      e = cudaMemcpyAsync(trace->treelets + lo * cap, d_tl + lo * cap, sizeof(uint32_t) * m * cap,
+                          cudaMemcpyDeviceToHost, s->xout);
+  }
+  if (st == RT_OK && e != cudaSuccess) st = cuda_fail(e, "rt_trace_host");
+  return host_finish(s, st);
 }
 
 }  // extern "C"

@@ -25,6 +25,20 @@ rt_status fail(rt_status s, const std::string& msg);
 // Host-side structural check of a blob; returns false with a message.
 bool validate_blob(const uint8_t* b, uint64_t n, std::string* err);
 
+// rt_trace_host runs a call of 2^20 rays or more as 4 chunks of 1/8, 3/8,
+// 3/8 and 1/8 of the rays (small first and last chunks shorten the copy-in
+// before the first trace and the copy-out after the last), one of 2^19 or
+// more as 2 halves, and smaller calls whole.  Each chunk costs about one
+// launch's tail (tens of microseconds on a full GPU), so more chunks lose.
+constexpr uint32_t kHostChunks = 4;
+inline uint32_t host_chunk_bounds(uint32_t n, uint64_t* lo) {
+  const uint32_t chunks = n >= (1u << 20) ? 4u : n >= (1u << 19) ? 2u : 1u;
+  static const uint32_t kEighths[3][5] = {{0, 8}, {0, 4, 8}, {0, 1, 4, 7, 8}};
+  const uint32_t* e = kEighths[chunks == 4 ? 2 : chunks - 1];
+  for (uint32_t c = 0; c <= chunks; ++c) lo[c] = (uint64_t)n * e[c] / 8;
+  return chunks;
+}
+
 // ---- bounce-ray construction (host and device) ----
 struct BounceInput {
   uint8_t leaf[64];
