@@ -327,12 +327,15 @@ struct PlainWalker {
     uint32_t c = ch.child_unit, nn = kNone;
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
+      // the first hit internal child becomes `next`; other hit children are
+      // pushed (one predicated store, no branch per child)
       const uint32_t info = ch.info_of(i);
-      if ((ch.hit_mask >> i) & 1u) {
-        if ((info >> 2) != rtf::CT_INTERNAL) push((c << 2) | level | kLeaf);
-        else if (nn == kNone) nn = c;
-        else push((c << 2) | level);
-      }
+      const bool h = (ch.hit_mask >> i) & 1u, internal = (info >> 2) == rtf::CT_INTERNAL;
+      const bool take = h && internal && nn == kNone, store = h && !take, ok = sp < CAP;
+      if (store && ok) stk[sp] = (c << 2) | level | (internal ? 0u : kLeaf);
+      if (store && !ok) status |= RT_RAY_STACK_OVERFLOW;
+      sp += (store && ok) ? 1 : 0;
+      nn = take ? c : nn;
       c += info & 3u;
     }
     next = nn;

@@ -14,25 +14,11 @@ constexpr uint32_t kSlotBitsDev = 10;
 constexpr uint32_t kEShift = 3, kEPin = 4;
 constexpr uint32_t kRouteOther = 6, kRouteInst = 12;  // route bits (treelets.h)
 
-// A LIFO stack of entries in local memory.  (Keeping the top entry in a
-// register measured slower on GB300: one more live 64-bit value per thread
-// costs more occupancy than the reload it saves.)
-template <int CAP>
-struct EStack {
-  unsigned long long e[CAP];
-  int n;
-  __device__ __forceinline__ bool push(unsigned long long v) {
-    if (n >= CAP) return false;
-    e[n++] = v;
-    return true;
-  }
-  __device__ __forceinline__ unsigned long long pop() { return e[--n]; }
-  __device__ __forceinline__ unsigned long long top() const { return e[n - 1]; }
-};
-
 // A ray's treelet-ordered walk.  Two LIFO stacks as in the reference
 // (push_front / pop_front on std::list, :1708-1709): `cu` holds nodes of the
-// current treelet, `ot` the rest (:1821-1856).  Which stack a child goes to
+// current treelet, `ot` the rest (:1821-1856).  Both live in one local
+// array (cu at [0, CAP), ot at [CAP, 2 CAP)), so that a push goes to either
+// with one predicated store instead of a branch per child.  Which stack a child goes to
 // is read from the per-node route bits (treelets.h): a node popped from `cu`
 // is in the current treelet, and a node popped from `ot` becomes the current
 // treelet root, so the reference's addrToTreeletID comparison is fixed per
@@ -45,7 +31,8 @@ struct Walker {
   float tmin, tmax, min_thit, c_tobj;
   bool terminate, fast, ic_fast;  // FAST min/max allowed for the world / object ray
   uint32_t c_leaf, c_inst, status;
-  EStack<CAP> cu, ot;
+  unsigned long long stk[2 * CAP];
+  int ncu, not_;  // entries on cu and on ot
   // The top of `cu` when it was pushed by the previous node visit: the node
   // the walk pops next, kept in a register instead of a local-memory round
   // trip (0 = none; no stack entry is 0, a blob's unit 0 is its TLAS header).
@@ -57,11 +44,11 @@ struct Walker {
   uint32_t pin_base;  // shared address of the pinned records, 0 = none
   uint32_t pin_root;  // record of the TLAS root node, 0 = not pinned
 
-  __device__ __forceinline__ bool active() const { return nxt != 0 || cu.n > 0 || ot.n > 0; }
+  __device__ __forceinline__ bool active() const { return nxt != 0 || (ncu | not_) != 0; }
 
   __device__ __forceinline__ void clear() {
     nxt = 0;
-    cu.n = ot.n = 0;
+    ncu = not_ = 0;
   }
 
   // Staged location (dense treelet << 10 | slot) of the node the ray visits
@@ -69,8 +56,8 @@ struct Walker {
   __device__ __forceinline__ uint32_t next_loc() const {
     unsigned long long e;
     if (nxt) e = nxt;
-    else if (cu.n > 0) e = cu.top();
-    else if (ot.n > 0) e = ot.top();
+    else if (ncu > 0) e = stk[ncu - 1];
+    else if (not_ > 0) e = stk[CAP + not_ - 1];
     else return kNone;
     if ((uint32_t)e & kEPin) return kNone;
     const uint32_t unit = (uint32_t)e >> kEShift;
@@ -79,12 +66,32 @@ struct Walker {
 
   __device__ __forceinline__ void push(bool same, uint32_t code, uint32_t inst) {
     const unsigned long long e = (unsigned long long)code | ((unsigned long long)inst << 32);
-    if (same) {
-      if (nxt && !cu.push(nxt)) status |= RT_RAY_STACK_OVERFLOW;
-      nxt = e;
-    } else if (!ot.push(e)) {
-      status |= RT_RAY_STACK_OVERFLOW;
+    // same treelet: e becomes nxt and the previous nxt (if any) goes to cu;
+    // else e goes to ot.  The staged walk (64 registers at 512 threads)
+    // measured faster with branches, the plain treelet walk with one
+    // predicated store.
+    if (STAGED) {
+      if (same) {
+        if (nxt) {
+          if (ncu < CAP) stk[ncu++] = nxt;
+          else status |= RT_RAY_STACK_OVERFLOW;
+        }
+        nxt = e;
+      } else if (not_ < CAP) {
+        stk[CAP + not_++] = e;
+      } else {
+        status |= RT_RAY_STACK_OVERFLOW;
+      }
+      return;
     }
+    const bool store = !same || nxt != 0;
+    const int cnt = same ? ncu : not_;
+    const bool ok = cnt < CAP;
+    if (store && ok) stk[same ? cnt : CAP + cnt] = same ? nxt : e;
+    if (store && !ok) status |= RT_RAY_STACK_OVERFLOW;
+    ncu += (same && store && ok) ? 1 : 0;
+    not_ += (!same && ok) ? 1 : 0;
+    nxt = same ? e : nxt;
   }
 
   __device__ __forceinline__ void bad_node() {
@@ -128,8 +135,13 @@ struct Walker {
   // of a node staged in a warp slot, else 0.
   template <class Lookup>
   __device__ __forceinline__ void step(const TraceArgs& a, Lookup&& lookup) {
-    const bool from_cu = nxt != 0 || cu.n > 0;  // :1748-1754
-    const unsigned long long e = nxt ? nxt : (from_cu ? cu.pop() : ot.pop());
+    const bool from_cu = nxt != 0 || ncu > 0;  // :1748-1754
+    unsigned long long e = nxt;
+    if (!nxt) {
+      e = stk[from_cu ? ncu - 1 : CAP + not_ - 1];
+      ncu -= from_cu ? 1 : 0;
+      not_ -= from_cu ? 0 : 1;
+    }
     nxt = 0;
     const uint32_t code = (uint32_t)e, inst = (uint32_t)(e >> 32);
     const bool top = code & kTop, leaf = code & kLeaf, pinned = STAGED && (code & kEPin);
