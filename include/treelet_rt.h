@@ -23,7 +23,8 @@
  *
  * Addresses: a node is named by its byte offset in the scene blob divided
  * by 64 (its "unit index"); the blob is one address space (the reference's
- * host-to-device offsets are 0).  A treelet is named by its root's unit index,
+ * host-to-device offsets are 0 unless rt_scene_set_device_offset says
+ * otherwise).  A treelet is named by its root's unit index,
  * exactly as the reference names a treelet by its root address.
  */
 #ifndef TREELET_RT_H
@@ -300,9 +301,9 @@ rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);
 /* Pinned treelets (RT_MODE_STAGED; no reference counterpart).  Each CTA of a
  * staged launch copies the pinned image into shared memory once, with
  * cp.async.bulk, and serves every read of a pinned node from it for the
- * whole launch.  The image holds the pinned treelets' nodes already decoded
- * (internal nodes as FP32 child bounds computed with the walk's own
- * operations), so results are unchanged.  Treelets are pinned in `order`
+ * whole launch.  The image holds the pinned nodes' own bytes with their
+ * route bits and the records of their pinned children, so results are
+ * unchanged.  Treelets are pinned in `order`
  * (dense ids, most wanted first) while they fit in tuning.pinned_bytes;
  * order == NULL restores the default order: the TLAS treelet, then treelets
  * by the surface-area probability of their root. */
@@ -315,6 +316,20 @@ typedef struct rt_pinned_info {
 } rt_pinned_info;
 /* The image the next staged launch uses, built now if needed. */
 rt_status rt_scene_pinned_info(rt_scene* scene, rt_pinned_info* info);
+
+/* The reference's device_offset: the shift from the host copy of the
+ * acceleration structure to the simulated device address that traceRay
+ * receives (vulkan_ray_tracing.cc:1549-1572).  Only zero versus nonzero
+ * changes a result.  0 (the default) gives the treelet order as intended.
+ * With a nonzero offset the reference stores a host address in
+ * current_treelet_root at the first pop from the other-treelet stack
+ * (:1752) but compares it with device treelet roots (:1821-1856,
+ * :1925-1936, :2015-2046), so from then on every child goes to the
+ * other-treelet stack; RT_MODE_TREELET and RT_MODE_STAGED then reproduce
+ * that order.  RT_MODE_PLAIN is unaffected.  Visit traces name blob units
+ * either way (the reference's transaction address is unit * 64 plus the
+ * offset). */
+rt_status rt_scene_set_device_offset(rt_scene* scene, uint64_t device_offset);
 
 /* Counters of the last rt_trace on this scene (read after the stream is
  * synchronised): node bytes read by the walk, bytes copied into shared memory

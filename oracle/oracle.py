@@ -127,7 +127,9 @@ class Treelets:
 def trace(blob: np.ndarray, rays: np.ndarray, mode: int = 0, treelets: Treelets | None = None, flags=None,
           default_flags: int = 1, capacity: int = 0, want_visits: bool = False, want_treelets: bool = False,
           threads: int = 1):
-    """mode 0 = traceRay, 1 = traceRayWithTreelets.  Returns (hits, visits, treelet ids)."""
+    """mode 0 = traceRay, 1 = traceRayWithTreelets (device_offset 0), 2 = traceRayWithTreelets with a
+    nonzero device_offset (every child after the first node goes to the other-treelet stack).
+    Returns (hits, visits, treelet ids)."""
     blob = np.ascontiguousarray(blob, np.uint8)
     if treelets is not None:
         # the partition is keyed by node addresses inside its own copy of the blob

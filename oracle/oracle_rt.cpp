@@ -657,9 +657,15 @@ void trace_plain(const uint8_t* tlas, uint32_t rayFlags, float3 origin, float Tm
   if (hit_procedural) out.hit.status |= RT_RAY_HIT_PROCEDURAL;
 }
 
-// traceRayWithTreelets (vulkan_ray_tracing.cc:1522-2307), device_offset = 0, no remap.
+// traceRayWithTreelets (vulkan_ray_tracing.cc:1522-2307), no remap.
+// offset_quirk = false: device_offset = 0.  offset_quirk = true: a nonzero
+// device_offset.  current_treelet_root starts as a device address (:1707)
+// but is then set from a stack entry's host address (:1752), while every
+// comparison looks up the child's device address (addrToTreeletID(child_addr
+// + device_offset), :1821-1856, :1925-1936, :2015-2046); after the first pop
+// no comparison can match, and every child goes to other_treelet_stack.
 void trace_treelets(const uint8_t* tlas, const oracle_treelets& T, uint32_t rayFlags, float3 origin, float Tmin,
-                    float3 direction, float Tmax, TraceOut& out) {
+                    float3 direction, float Tmax, TraceOut& out, bool offset_quirk) {
   const bool terminateOnFirstHit = rayFlags & RT_RAY_FLAG_TERMINATE_ON_FIRST_HIT;
   auto& transactions = out.transactions;
   bool hit_procedural = false;
@@ -677,6 +683,7 @@ void trace_treelets(const uint8_t* tlas, const oracle_treelets& T, uint32_t rayF
   transactions.push_back({tlas, RT_TX_STRUCTURE});
   const uint8_t* topRootAddr = tlas + topBVH.RootNodeOffset;
   const uint8_t* current_treelet_root = tlas;  // :1707
+  bool root_is_device_address = true;           // false once :1752 stores a host address (offset_quirk)
   std::list<StackEntry> current_treelet_stack, other_treelet_stack;
   {
     float thit;
@@ -689,7 +696,7 @@ void trace_treelets(const uint8_t* tlas, const oracle_treelets& T, uint32_t rayF
     }
   }
   auto route = [&](const StackEntry& e) {
-    if (current_treelet_root == T.addrToTreeletID(e.addr))
+    if (root_is_device_address && current_treelet_root == T.addrToTreeletID(e.addr))
       current_treelet_stack.push_front(e);
     else
       other_treelet_stack.push_front(e);
@@ -698,6 +705,7 @@ void trace_treelets(const uint8_t* tlas, const oracle_treelets& T, uint32_t rayF
     if (current_treelet_stack.empty()) {  // :1748-1754
       current_treelet_stack.push_front(other_treelet_stack.front());
       current_treelet_root = other_treelet_stack.front().addr;
+      if (offset_quirk) root_is_device_address = false;
       other_treelet_stack.pop_front();
     }
     StackEntry cur = current_treelet_stack.front();
@@ -826,7 +834,7 @@ void trace_range(const uint8_t* blob, const oracle_treelets* tl, const rt_ray* r
     if (mode == 0)
       trace_plain(blob, f, org, ry.tmin, dir, ry.tmax, o);
     else
-      trace_treelets(blob, *tl, f, org, ry.tmin, dir, ry.tmax, o);
+      trace_treelets(blob, *tl, f, org, ry.tmin, dir, ry.tmax, o, mode == 2);
     if (capacity && o.transactions.size() > capacity) o.hit.status |= RT_RAY_TRACE_OVERFLOW;
     hits[r] = o.hit;
     const size_t m = std::min<size_t>(o.transactions.size(), capacity);
@@ -972,7 +980,11 @@ int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* t
                  const uint32_t* flags, uint32_t default_flags, uint64_t n, int mode, rt_hit* hits, uint32_t* visits,
                  uint32_t* treelets, uint32_t capacity, int threads) {
   (void)n_bytes;
-  if ((mode == 1 || treelets) && !tl) {
+  if (mode < 0 || mode > 2) {
+    g_err = "oracle_trace: mode must be 0, 1 or 2";
+    return -1;
+  }
+  if ((mode != 0 || treelets) && !tl) {
     g_err = "oracle_trace: treelets required";
     return -1;
   }

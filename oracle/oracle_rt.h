@@ -45,7 +45,10 @@ void oracle_treelets_get(const oracle_treelets* t, uint64_t n_units, uint32_t* r
 int oracle_remap(const oracle_treelets* t, int max_bytes, uint32_t stride, uint64_t n_units, uint64_t* new_addr);
 
 /* Traces n rays with traceRay (mode 0, :2309-3076) or traceRayWithTreelets
- * (mode 1, :1522-2307).  `tl` is required for mode 1 and for treelet traces.
+ * (mode 1, :1522-2307, device_offset = 0; mode 2, the same with a nonzero
+ * device_offset, where every child after the first node goes to the
+ * other-treelet stack).  `tl` is required for modes 1 and 2 and for treelet
+ * traces.
  * visits / treelets / capacity follow rt_trace_buf.  threads <= 1 runs on the
  * calling thread, otherwise contiguous ray ranges per std::thread.
  * Returns 0 or -1 (message in oracle_last_error). */

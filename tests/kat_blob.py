@@ -121,3 +121,16 @@ TREELET_TERMINATE = [(0, S), (1, I), (2, IL), (4, S), (5, I), (8, D), (8, H)]
 ROOTS_256 = [0, 2, 6, 7, 8, 15]
 MEMBERS_256 = [[0, 1], [2, 4, 5], [6, 9, 10, 11], [7, 12, 13, 14], [8], [15]]
 TREELET_IDS_256 = [0, 0, 2, 2, 2, 8, 8, 7, 6]
+# Budget 192: the partition is [0, 1], [2, 4], [5, 6, 7] and one-node treelets
+# for every leaf.  A's children B and C share A's treelet; L0 does not.
+ROOTS_192 = [0, 2, 5, 8, 9, 10, 11, 12, 13, 14, 15]
+# device_offset = 0: B and C go to the current-treelet stack, L0 to the other
+# one, so C and B (LIFO) are walked before L0, and every leaf of C and B is
+# reached before the closest hit L0 culls anything.
+TREELET_192 = [(0, S), (1, I), (2, IL), (4, S), (5, I), (7, I), (6, I), (11, D), (11, H), (10, D), (10, H), (9, D),
+               (9, H), (15, D), (15, Q), (14, D), (14, Q), (13, D), (13, Q), (12, D), (12, Q), (8, D), (8, H)]
+# Nonzero device_offset (vulkan_ray_tracing.cc:1752): after the instance leaf
+# is moved from the other stack no comparison matches, so B, C and L0 all go to
+# the other stack and L0, pushed last, is walked first; its hit at t = 6 culls
+# every leaf of C and B.
+TREELET_192_OFFSET = [(0, S), (1, I), (2, IL), (4, S), (5, I), (8, D), (8, H), (7, I), (6, I)]

@@ -17,6 +17,8 @@ def _scenes(ctx):
         blob = rt.Blob.gen(kind, n, seed)
         scene = rt.Scene(ctx, blob)
         scene.form_treelets(8192)
+        if kind == rt.SCENE_TERRAIN_INSTANCES:  # a batch carries each scene's own walk
+            scene.set_device_offset(1 << 40)
         cam = rt.default_camera(kind)
         rays = rt.camera_rays(cam, 40 + 8 * seed, 30 + 4 * seed, 1, seed, 1e-4, 1e30)
         out.append((scene, rays))

@@ -251,3 +251,44 @@ def test_host_trace_chunks_match_device_trace(ctx, n):
         assert host_stats["node_bytes"] == dev_stats["node_bytes"] > 0, name
         assert host_stats["device_status"] == dev_stats["device_status"] == 0, name
     scene.close()
+
+
+def test_device_offset_walk(ctx):
+    """rt_scene_set_device_offset(nonzero) reproduces the treelet order of the
+    reference's nonzero device_offset (oracle mode 2) in the treelet and staged
+    walks, on the hand-derived KAT and on generated scenes; 0 restores the
+    intended order."""
+    import kat_blob as K
+
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    kat = rt.Blob.wrap(K.kat_blob())
+    scene = rt.Scene(ctx, kat)
+    scene.form_treelets(192)
+    for offset, expect in ((1 << 32, K.TREELET_192_OFFSET), (0, K.TREELET_192)):
+        scene.set_device_offset(offset)
+        for mode in (rt.MODE_TREELET, rt.MODE_STAGED):
+            hits, vis, _ = scene.trace_host(K.kat_ray(), mode, capacity=64, want_visits=True)
+            n = int(hits["n_visits"][0])
+            assert [(int(x) >> 3, int(x) & 7) for x in vis[0, :n]] == expect, (offset, mode)
+    scene.close()
+
+    cases = [(rt.SCENE_CUBE_PLANE, 16384, 96, 2048), (rt.SCENE_TERRAIN_INSTANCES, 2 * 64 * 64, 64, 8192)]
+    for kind, n_tris, side, budget in cases:
+        blob = rt.Blob.gen(kind, n_tris, 3)
+        prim = rt.camera_rays(rt.default_camera(kind), side, side, 1, 2, 1e-4, 1e30)
+        ph, _, _ = orc.trace(blob.bytes(), prim, 0)
+        rays = np.concatenate([prim, rt.bounce_rays_host(blob, prim, ph, seed=5)])
+        tl = orc.Treelets(blob.bytes(), budget)
+        oh, ov, ot = orc.trace(blob.bytes(), rays, 2, tl, capacity=CAP, want_visits=True, want_treelets=True,
+                               threads=8)
+        scene = rt.Scene(ctx, blob)
+        scene.form_treelets(budget)
+        scene.set_device_offset(12345)
+        for mode, name in ((rt.MODE_TREELET, "treelet"), (rt.MODE_STAGED, "staged")):
+            hits, vis, tids = scene.trace_host(rays, mode, capacity=CAP, want_visits=True, want_treelets=True)
+            assert_hits_equal(hits, oh, f"{name} hits, device offset")
+            assert_traces_equal(vis, ov, oh["n_visits"], f"{name} visits, device offset")
+            assert_traces_equal(tids, ot, oh["n_visits"], f"{name} treelet ids, device offset")
+        scene.close()

@@ -70,6 +70,27 @@ def test_treelet_walk(budget):
     assert pairs == K.TREELET_TERMINATE
 
 
+def test_treelet_walk_device_offset():
+    """traceRayWithTreelets with a nonzero device_offset (oracle mode 2): the
+    first pop from the other stack stores a host address in
+    current_treelet_root (:1752) and no later comparison matches."""
+    from oracle import oracle as orc
+
+    tl = orc.Treelets(K.kat_blob(), 192)
+    assert tl.get()["roots"].tolist() == K.ROOTS_192
+    for flags in (1, 0):  # the treelet walk keeps a closer hit whatever the Opaque flag (:2127)
+        _, pairs, _ = _trace(1, flags, tl)
+        assert pairs == K.TREELET_192
+        _, pairs, _ = _trace(2, flags, tl)
+        assert pairs == K.TREELET_192_OFFSET
+    # before the first move the comparisons still see device addresses, so at
+    # these budgets both walks agree
+    for budget in (256, 8192):
+        tl = orc.Treelets(K.kat_blob(), budget)
+        _, pairs, _ = _trace(2, 1, tl)
+        assert pairs == K.TREELET_OPAQUE
+
+
 def test_remap_256():
     from oracle import oracle as orc
 

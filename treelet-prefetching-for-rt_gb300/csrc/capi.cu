@@ -111,6 +111,7 @@ struct rt_scene {
   uint32_t* d_hint = nullptr;  // staged-mode predictions (8 per treelet) or null
   uint32_t slot_bytes = 0;
   std::vector<uint16_t> route;  // routing bits of the treelet-ordered walk
+  bool offset_quirk = false;    // walk as the reference does with a nonzero device_offset
   uint16_t* d_route = nullptr;
   // pinned treelets of the staged walk (built when treelets, order or budget change)
   std::vector<uint32_t> pin_order;  // explicit order, empty = default
@@ -232,6 +233,25 @@ int max_smem_per_block() {
 uint32_t staged_smem_limit() {
   const int v = max_smem_per_block() - (int)(sizeof(rtk::WarpStage) * (rtk::kStagedMaxThreads / 32)) - 1024;
   return v > 0 ? (uint32_t)v : 0u;
+}
+
+rt_status rebuild_pinned(rt_scene* s);
+
+// Computes the route bits of the walk (treelets.h) into s->route, uploads
+// them and rebuilds the pinned image that embeds them.  With a nonzero
+// device_offset the reference's comparisons stop matching at the first pop
+// from the other-treelet stack (vulkan_ray_tracing.cc:1752); the current
+// stack is empty then and nothing is pushed to it again, so every later node
+// is popped from the other stack.  Clearing the bits a node popped from the
+// other stack reads (6-11 and 13) therefore gives that walk, while a node
+// popped from the current stack, which happens only before the first such
+// pop, keeps its comparisons.
+rt_status upload_route(rt_scene* s) {
+  rtt::route_masks(s->host_blob.data(), s->blob_bytes, s->part, s->route);
+  if (s->offset_quirk)
+    for (uint16_t& r : s->route) r &= (uint16_t)~((0x3Fu << rtt::kRouteOtherShift) | (2u << rtt::kRouteInstShift));
+  RT_CUDA(cudaMemcpy(s->d_route, s->route.data(), sizeof(uint16_t) * s->route.size(), cudaMemcpyHostToDevice));
+  return rebuild_pinned(s);
 }
 
 // Rebuilds the pinned image for the scene's order and budget (the budget is
@@ -503,15 +523,13 @@ rt_status rt_treelets_form(rt_scene* s, uint32_t max_treelet_bytes, rt_treelet_i
     RT_CUDA(cudaMemcpy(s->d_members, p.members.data(), sizeof(uint32_t) * p.members.size(), cudaMemcpyHostToDevice));
   s->slot_bytes = (p.largest_image + 127u) & ~127u;
   s->part = std::move(p);
-  rtt::route_masks(s->host_blob.data(), s->blob_bytes, s->part, s->route);
-  st = dalloc(&s->d_route, sizeof(uint16_t) * s->route.size());
+  st = dalloc(&s->d_route, sizeof(uint16_t) * (s->blob_bytes / 64));
   if (st != RT_OK) {
     free_treelets(s);
     return st;
   }
-  RT_CUDA(cudaMemcpy(s->d_route, s->route.data(), sizeof(uint16_t) * s->route.size(), cudaMemcpyHostToDevice));
   s->has_treelets = true;
-  st = rebuild_pinned(s);
+  st = upload_route(s);
   if (st != RT_OK) {
     free_treelets(s);
     return st;
@@ -572,6 +590,15 @@ rt_status rt_scene_set_pin_order(rt_scene* s, const uint32_t* order, uint32_t n)
   else s->pin_order.clear();
   RT_CUDA(cudaSetDevice(s->ctx->device));
   return rebuild_pinned(s);
+}
+
+rt_status rt_scene_set_device_offset(rt_scene* s, uint64_t device_offset) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_scene_set_device_offset: NULL scene");
+  if (s->offset_quirk == (device_offset != 0)) return RT_OK;
+  s->offset_quirk = device_offset != 0;
+  if (!s->has_treelets) return RT_OK;
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  return upload_route(s);
 }
 
 rt_status rt_scene_pinned_info(rt_scene* s, rt_pinned_info* info) {

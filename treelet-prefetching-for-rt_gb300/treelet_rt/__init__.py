@@ -274,6 +274,11 @@ class Scene:
         o = np.ascontiguousarray(order, np.uint32)
         check(lib().rt_scene_set_pin_order(self._h, o.ctypes.data, len(o)))
 
+    def set_device_offset(self, device_offset: int) -> None:
+        """The reference's host-to-device address offset: nonzero reproduces the treelet order the
+        reference walks with one (every child after the first node to the other-treelet stack)."""
+        check(lib().rt_scene_set_device_offset(self._h, device_offset))
+
     def pinned_info(self) -> dict:
         info = PinnedInfo()
         check(lib().rt_scene_pinned_info(self._h, C.byref(info)))

@@ -148,6 +148,7 @@ PROTOTYPES = {
     "rt_scene_set_pin_order": (C.c_int, [vp, vp, C.c_uint32]),
     "rt_unit_replay": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.POINTER(UnitConfig), vp, vp]),
     "rt_scene_pinned_info": (C.c_int, [vp, C.POINTER(PinnedInfo)]),
+    "rt_scene_set_device_offset": (C.c_int, [vp, C.c_uint64]),
     "rt_trace_host_noalloc": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
     "rt_batch_create": (C.c_int, [vp, C.POINTER(vp), C.c_uint32, C.POINTER(vp)]),
     "rt_batch_destroy": (C.c_int, [vp]),
