@@ -432,6 +432,10 @@ struct PlainWalker {
   }
 };
 
+// The plain walk keeps its stack inside the walker, whose fields the compiler
+// then leaves in local memory: 48 registers and five 256-thread CTAs per SM.
+// Its fields in registers (90, or capped at 51-85 with spills) measured
+// 40-45% slower, while the treelet walks gained from them (below).
 template <int CAP>
 __global__ void __launch_bounds__(256) trace_plain_kernel(TraceArgs a) {
   PlainWalker<CAP> w;
