@@ -338,13 +338,15 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
   RT_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), st));
   if (mode == RT_MODE_PLAIN) {
     const uint32_t bt = t.block_threads;
-    auto kern = rtk::trace_plain_kernel<CAP>;
+    auto kern = a.n_items ? rtk::trace_plain_kernel<CAP, true> : rtk::trace_plain_kernel<CAP, false>;
     kern<<<persistent_grid((const void*)kern, bt, a.n), bt, 0, st>>>(a);
   } else if (mode == RT_MODE_TREELET) {
     const uint32_t bt = t.block_threads;
-    auto kern = rtk::trace_treelet_kernel<CAP>;
+    auto kern = a.n_items ? rtk::trace_treelet_kernel<CAP, true> : rtk::trace_treelet_kernel<CAP, false>;
     kern<<<persistent_grid((const void*)kern, bt, a.n), bt, 0, st>>>(a);
   } else {
+    // the staged kernel is compiled for launches over one scene
+    if (a.n_items) return rti::fail(RT_ERR_INVALID, "staged traces run over one scene");
     const uint32_t bt = t.staged_threads;
     const uint32_t warps = bt / 32;
     // per-warp slots: the whole largest image, or the first staged_slot_bytes of each

@@ -104,9 +104,11 @@ __device__ __forceinline__ void load_ray(const rt_ray* rays, uint32_t r, rtm::V3
   tmax = b.w;
 }
 
-// The scene ray r walks.
+// The scene ray r walks.  MULTI = false compiles a launch over one scene,
+// whose tables are the launch arguments themselves.
+template <bool MULTI>
 __device__ __forceinline__ SceneView scene_of(const TraceArgs& a, uint32_t r) {
-  if (a.n_items == 0) return SceneView{a.blob, a.meta, a.route, a.n_units};
+  if (!MULTI || a.n_items == 0) return SceneView{a.blob, a.meta, a.route, a.n_units};
   uint32_t lo = 0, hi = a.n_items;  // last item with item_begin <= r
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
@@ -256,7 +258,7 @@ __device__ __forceinline__ void run_persistent(const TraceArgs& a, W& w, unsigne
 // the internal node descended next (the first hit internal child, :2570-2578);
 // leaves and further children are pushed.  A top-level instance leaf is
 // followed by its whole BLAS before the next top-level entry (:2602-2679).
-template <int CAP>
+template <int CAP, bool MULTI>
 struct PlainWalker {
   rtm::V3 O, D, idir;
   float tmin, tmax, min_thit, c_tobj;
@@ -279,7 +281,7 @@ struct PlainWalker {
   __device__ __forceinline__ uint32_t pop() { return stk[--sp]; }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
-    v = scene_of(a, r);
+    v = scene_of<MULTI>(a, r);
     load_ray(a.rays, r, O, tmin, D, tmax);
     const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
     terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
@@ -436,9 +438,9 @@ struct PlainWalker {
 // then leaves in local memory: 48 registers and five 256-thread CTAs per SM.
 // Its fields in registers (90, or capped at 51-85 with spills) measured
 // 40-45% slower, while the treelet walks gained from them (below).
-template <int CAP>
+template <int CAP, bool MULTI>
 __global__ void __launch_bounds__(256) trace_plain_kernel(TraceArgs a) {
-  PlainWalker<CAP> w;
+  PlainWalker<CAP, MULTI> w;
   unsigned long long bytes = 0;
   run_persistent(a, w, bytes);
   if (a.stats) add_warp_total64(a.stats + ST_NODE_BYTES, bytes);

@@ -25,7 +25,7 @@ constexpr uint32_t kRouteOther = 6, kRouteInst = 12;  // route bits (treelets.h)
 // node and precomputed.  The staged location of a node (dense treelet << 10 |
 // 64-byte slot in that treelet's image) is read from the node table when a
 // warp has a staged slot; pinned nodes are named by their record.
-template <int CAP, bool STAGED>
+template <int CAP, bool STAGED, bool MULTI>
 struct Walker {
   rtm::V3 O, D, idir;
   float tmin, tmax, min_thit, c_tobj;
@@ -100,7 +100,7 @@ struct Walker {
   }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
-    v = scene_of(a, r);
+    v = scene_of<MULTI>(a, r);
     load_ray(a.rays, r, O, tmin, D, tmax);
     const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
     terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
@@ -302,10 +302,10 @@ struct Walker {
 // memory), and better than caps of 51 or 64 (spills) or none (99 registers).
 constexpr int kTreeletMinBlocks = 3;
 
-template <int CAP>
+template <int CAP, bool MULTI>
 __global__ void __launch_bounds__(256, kTreeletMinBlocks) trace_treelet_kernel(TraceArgs a) {
   unsigned long long stack[2 * CAP];
-  Walker<CAP, false> w;
+  Walker<CAP, false, MULTI> w;
   w.stk = stack;
   w.pin_base = 0;
   w.pin_root = 0;
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_sta
     return 0u;
   };
   unsigned long long stack[2 * CAP];
-  Walker<CAP, true> w;
+  Walker<CAP, true, false> w;  // staged launches trace one scene
   w.stk = stack;
   w.pin_base = pin_ok ? smem_u32(smem0) : 0u;
   w.pin_root = pin_ok ? a.pin_root : 0u;
