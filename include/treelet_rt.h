@@ -286,7 +286,7 @@ rt_status rt_scene_set_stage_hints(rt_scene* scene, const uint32_t* hints);
 #define RT_TUNING_OFF 0xFFFFFFFFu
 typedef struct rt_tuning {
   uint32_t block_threads;     /* threads per CTA for RT_MODE_PLAIN / RT_MODE_TREELET (32..256) */
-  uint32_t staged_threads;    /* threads per CTA for RT_MODE_STAGED (32..512) */
+  uint32_t staged_threads;    /* threads per CTA for RT_MODE_STAGED (32..256) */
   uint32_t staged_epoch;      /* node visits of a warp between staging votes */
   uint32_t staged_slots;      /* shared-memory treelet slots per warp (1..8; RT_TUNING_OFF: none) */
   uint32_t refill_lanes;      /* idle lanes of a warp that make it fetch new rays (1..32) */

@@ -134,3 +134,73 @@ TREELET_192 = [(0, S), (1, I), (2, IL), (4, S), (5, I), (7, I), (6, I), (11, D),
 # the other stack and L0, pushed last, is walked first; its hit at t = 6 culls
 # every leaf of C and B.
 TREELET_192_OFFSET = [(0, S), (1, I), (2, IL), (4, S), (5, I), (8, D), (8, H), (7, I), (6, I)]
+
+
+# ---------------------------------------------------------------- edge cases
+# Axis-parallel rays on a box face, derived by hand from calculate_idir
+# (vulkan_ray_tracing.cc:220-235), ray_box_test (:237-257) and the MIN/MAX
+# ternaries.  The ray (-5, 0, 8) -> +x runs in the top face z = 8 of the TLAS
+# and BLAS boxes, so its z slab is decided by the sign of its zero z direction:
+#   d.z = +0: idir.z = +2^80, the z slab is [-7 * 2^80, 0]; tfar = 0 < tnear = 4,
+#             and the TLAS header box is missed: one STRUCTURE visit.
+#   d.z = -0: idir.z = -2^80, the z slab is [-0, 7 * 2^80]; the header and the
+#             TLAS root's instance box are hit at t = 4.  The identity
+#             world-to-object product then turns the direction's -0 into +0
+#             (0.0f + 1 * -0.0f = +0, float4x4::operator*), so in object space
+#             the ray misses every child of the BLAS root A (B's z slab ends at
+#             -4 * 2^80, C's and L0's at <= 0): no hit.
+def face_ray(dz_sign: float):
+    from treelet_rt import RAY_DTYPE
+
+    r = np.zeros(1, RAY_DTYPE)
+    r["origin"] = (-5.0, 0.0, 8.0)
+    r["dir"] = (1.0, 0.0, np.copysign(0.0, dz_sign))
+    r["tmin"] = 1e-4
+    r["tmax"] = 1e30
+    return r
+
+
+FACE_POS_ZERO = [(0, S)]
+FACE_NEG_ZERO = [(0, S), (1, I), (2, IL), (4, S), (5, I)]
+
+
+# A ray in the plane of a triangle: mt_ray_triangle_test (:3089-3111) has no
+# epsilon on the determinant, so det = 0 gives idet = +inf, u = v = thit =
+# 0 * inf = NaN; NaN passes both rejection tests (u < 0 || u > 1 and
+# v < 0 || u + v > 1 are false), the test returns true with thit = NaN, and
+# the range check tmin <= t <= tmax (:2843) rejects it: the leaf is recorded
+# as QUAD_LEAF (a miss) and the ray reports no hit.
+#
+#     unit 0   TLAS header     root at unit 1, bounds [-1,3]x[-1,3]x[0,2]
+#     unit 1   TLAS root       one child: the instance leaf
+#     units 2-3 instance leaf  identity, InstanceID 9, BLAS header at unit 4
+#     unit 4   BLAS header     root at unit 5
+#     unit 5   BLAS root       one child: the quad leaf, box z in [0, 2]
+#     unit 6   quad leaf       triangle (-1,-1,1) (3,-1,1) (-1,3,1), PrimitiveIndex0 200
+def coplanar_blob() -> np.ndarray:
+    box = [(2, 1, (0, 0, 0), (64, 64, 32))]
+    units = [
+        _header(64, (-1, -1, 0), (3, 3, 2)),
+        _internal((-1, -1, 0), 1, (4, 4, 4), box),
+        _instance(2 * 64, 9),
+        _header(64, (-1, -1, 0), (3, 3, 2)),
+        _internal((-1, -1, 0), 1, (4, 4, 4), [(1, 4, (0, 0, 0), (64, 64, 32))]),
+        _quad(1.0, 200),
+    ]
+    blob = b"".join(units)
+    assert len(blob) == 7 * 64
+    return np.frombuffer(blob, np.uint8).copy()
+
+
+def coplanar_ray():
+    from treelet_rt import RAY_DTYPE
+
+    r = np.zeros(1, RAY_DTYPE)
+    r["origin"] = (-5.0, 0.0, 1.0)
+    r["dir"] = (1.0, 0.0, 0.0)
+    r["tmin"] = 1e-4
+    r["tmax"] = 1e30
+    return r
+
+
+COPLANAR = [(0, S), (1, I), (2, IL), (4, S), (5, I), (6, D), (6, Q)]

@@ -110,6 +110,26 @@ def test_edge_rays(ctx):
     _check_all_modes(ctx, blob, edge_rays())
 
 
+def test_hand_derived_edge_cases(ctx):
+    """The signed-zero box-face rays and the zero-determinant ray of
+    kat_blob.py, in every mode, against their hand-derived visits."""
+    import kat_blob as K
+
+    import treelet_rt as rt
+
+    cases = [(K.kat_blob(), K.face_ray(+1.0), K.FACE_POS_ZERO), (K.kat_blob(), K.face_ray(-1.0), K.FACE_NEG_ZERO),
+             (K.coplanar_blob(), K.coplanar_ray(), K.COPLANAR)]
+    for blob, ray, expect in cases:
+        scene = rt.Scene(ctx, rt.Blob.wrap(blob))
+        scene.form_treelets(8192)
+        for mode in (rt.MODE_PLAIN, rt.MODE_TREELET, rt.MODE_STAGED):
+            hits, vis, _ = scene.trace_host(ray, mode, capacity=64, want_visits=True)
+            n = int(hits["n_visits"][0])
+            assert [(int(x) >> 3, int(x) & 7) for x in vis[0, :n]] == expect, mode
+            assert hits["hit_geometry"][0] == 0
+        scene.close()
+
+
 def test_trace_overflow_truncates(ctx):
     import treelet_rt as rt
 
@@ -138,7 +158,7 @@ OFF = 0xFFFFFFFF
 @pytest.mark.parametrize("tuning", [dict(pinned_bytes=OFF),
                                     dict(pinned_bytes=1024, staged_slots=OFF),
                                     dict(pinned_bytes=16384, staged_epoch=1, staged_min_votes=1),
-                                    dict(pinned_bytes=200000, staged_slots=OFF, staged_threads=512),
+                                    dict(pinned_bytes=200000, staged_slots=OFF, staged_threads=256),
                                     dict(pinned_bytes=65536, staged_threads=256, staged_slots=2, refill_lanes=1)])
 @pytest.mark.parametrize("scene_kind", ["terrain", "shared_blas", "bounce"])
 def test_pinned_treelets_invariance(ctx, tuning, scene_kind):

@@ -142,3 +142,38 @@ def test_quantization_round_trip():
                     assert (v >= np.array(lo_, np.float32)).all() and (v <= np.array(hi_, np.float32)).all()
                 leaves += 1
     assert leaves == 3002
+
+
+def _trace_blob(blob, ray, mode, flags=1, tl=None):
+    from oracle import oracle as orc
+
+    hits, vis, _ = orc.trace(blob, ray, mode, tl, default_flags=flags, capacity=64, want_visits=True)
+    n = int(hits["n_visits"][0])
+    return hits[0], [(int(v) >> 3, int(v) & 7) for v in vis[0, :n]]
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_signed_zero_direction_on_a_box_face(mode):
+    """An axis-parallel ray in a box face: the sign of its zero direction
+    component decides the slab test, and the instance transform turns -0
+    into +0 (hand-derived in kat_blob.py)."""
+    from oracle import oracle as orc
+
+    tl = orc.Treelets(K.kat_blob(), 8192) if mode else None
+    h, pairs = _trace_blob(K.kat_blob(), K.face_ray(+1.0), mode, tl=tl)
+    assert pairs == K.FACE_POS_ZERO and h["hit_geometry"] == 0
+    h, pairs = _trace_blob(K.kat_blob(), K.face_ray(-1.0), mode, tl=tl)
+    assert pairs == K.FACE_NEG_ZERO and h["hit_geometry"] == 0
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_zero_determinant_is_a_miss(mode):
+    """A ray in the triangle's plane: det = 0, the NaN distance passes the
+    barycentric tests and fails the range check (hand-derived in kat_blob.py)."""
+    from oracle import oracle as orc
+
+    blob = K.coplanar_blob()
+    tl = orc.Treelets(blob, 8192) if mode else None
+    for flags in (1, 0):
+        h, pairs = _trace_blob(blob, K.coplanar_ray(), mode, flags=flags, tl=tl)
+        assert pairs == K.COPLANAR and h["hit_geometry"] == 0

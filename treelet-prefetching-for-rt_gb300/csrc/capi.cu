@@ -289,7 +289,8 @@ rt_status merge_tuning(const rt_tuning& cur, const rt_tuning* t, rt_tuning& n) {
   }
   if (t->staged_threads) {
     if (!ok_threads(t->staged_threads, rtk::kStagedMaxThreads))
-      return rti::fail(RT_ERR_INVALID, "staged_threads must be 32..512, multiple of 32");
+      return rti::fail(RT_ERR_INVALID, "staged_threads must be 32.." + std::to_string(rtk::kStagedMaxThreads) +
+                                           ", multiple of 32");
     n.staged_threads = t->staged_threads;
   }
   if (t->staged_epoch) n.staged_epoch = t->staged_epoch;

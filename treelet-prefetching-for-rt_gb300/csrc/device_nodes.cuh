@@ -1,4 +1,4 @@
-// Device-side node access: 16-byte vector loads of the 64 / 128-byte nodes
+// Device-side node access: 32-byte vector loads of the 64 / 128-byte nodes
 // from global memory (read-only path) or from a staged shared-memory image,
 // and the decoders for the fields the walk uses (format.h).
 #pragma once
@@ -29,8 +29,23 @@ __device__ __forceinline__ uint32_t ld_shared_u32(uint32_t saddr) {
   return v;
 }
 
+// One 32-byte read-only load from global memory (256-bit loads exist on
+// sm_100 and later, for the global state space only): a 64-byte node takes
+// two load instructions instead of four.  p must be 32-byte aligned; nodes are
+// 64-byte aligned in the blob.
+__device__ __forceinline__ void ld_global_v8(const uint4* p, uint32_t* w) {
+  asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+      : "l"(p));
+}
+
 // Loads 64 bytes: from shared memory when saddr != 0, else from global.
 __device__ __forceinline__ void load64(const uint4* g, uint32_t saddr, Node64& n) {
+  if (!saddr) {
+    ld_global_v8(g, n.w);
+    ld_global_v8(g + 2, n.w + 8);
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const uint4 v = saddr ? ld_shared_v4(saddr + 16u * q) : ld_global_nc(g + q);

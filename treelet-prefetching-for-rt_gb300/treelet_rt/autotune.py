@@ -24,7 +24,7 @@ GRID_COMMON = {
 }
 OFF = 0xFFFFFFFF  # RT_TUNING_OFF
 GRID_STAGED = {
-    "staged_threads": [128, 256, 512],
+    "staged_threads": [64, 128, 256],
     "refill_lanes": [4, 8, 16, 32],
     "pinned_bytes": [OFF, 4096, 16384, 65536],
     "staged_slots": [OFF, 1, 2, 4],
