@@ -67,6 +67,8 @@ def lib():
         L.oracle_prefetch_decide.argtypes = [vp, vp, C.c_uint32, C.POINTER(_Params), vp, vp]
         L.oracle_decode_node.restype = C.c_int
         L.oracle_decode_node.argtypes = [vp, C.c_uint32, C.c_int, vp]
+        L.oracle_geometry.restype = C.c_int
+        L.oracle_geometry.argtypes = [C.c_int, vp, C.c_uint32, vp]
         L.oracle_unit_replay.restype = C.c_int
         L.oracle_unit_replay.argtypes = [vp, C.c_int, C.c_uint64, vp, vp, C.c_uint32, C.c_uint32, vp, vp, C.c_int]
         _lib = L
@@ -78,6 +80,20 @@ def decode_node(blob: np.ndarray, unit: int, kind: int) -> np.ndarray:
     blob = np.ascontiguousarray(blob, np.uint8)
     out = np.zeros(62, np.float64)
     if lib().oracle_decode_node(blob.ctypes.data, unit, kind, out.ctypes.data) != 0:
+        raise OracleError(lib().oracle_last_error().decode())
+    return out
+
+
+GEOMETRY_IN = (14, 17, 24, 12)
+GEOMETRY_OUT = (5, 2, 9, 3)
+
+
+def geometry(op: int, cases: np.ndarray) -> np.ndarray:
+    """The oracle's ray geometry on cases (rows of GEOMETRY_IN[op] float32),
+    in the layouts of oracle/ref_pin/pin_geometry.cpp."""
+    cases = np.ascontiguousarray(cases, np.float32).reshape(-1, GEOMETRY_IN[op])
+    out = np.zeros((len(cases), GEOMETRY_OUT[op]), np.float32)
+    if lib().oracle_geometry(op, cases.ctypes.data, len(cases), out.ctypes.data) != 0:
         raise OracleError(lib().oracle_last_error().decode())
     return out
 

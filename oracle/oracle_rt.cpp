@@ -854,6 +854,50 @@ void trace_range(const uint8_t* blob, const oracle_treelets* tl, const rt_ray* r
 
 extern "C" {
 
+// The oracle's ray geometry on a batch of cases, in the case and result
+// layouts of oracle/ref_pin/pin_geometry.cpp (which runs the reference's own
+// functions): op 0 calculate_idir + ray_box_test, 1 mt_ray_triangle_test,
+// 2 make_transformed_ray, 3 Barycentric.  Returns 0 or -1.
+int oracle_geometry(int op, const float* in, uint32_t n, float* out) {
+  static const int kIn[4] = {14, 17, 24, 12}, kOut[4] = {5, 2, 9, 3};
+  if (op < 0 || op > 3) {
+    g_err = "oracle_geometry: op must be 0..3";
+    return -1;
+  }
+  auto f3 = [](const float* p) { return float3{p[0], p[1], p[2]}; };
+  for (uint32_t k = 0; k < n; ++k) {
+    const float* c = in + (size_t)k * kIn[op];
+    float* o = out + (size_t)k * kOut[op];
+    if (op == 0) {
+      const float3 idir = calculate_idir(f3(c + 9));
+      float thit = -1.0f;
+      const bool hit = ray_box_test(f3(c), f3(c + 3), idir, f3(c + 6), c[12], c[13], thit);
+      o[0] = idir.x, o[1] = idir.y, o[2] = idir.z, o[3] = hit ? 1.0f : 0.0f, o[4] = thit;
+    } else if (op == 1) {
+      Ray r;
+      r.make_ray(f3(c + 9), f3(c + 12), c[15], c[16]);
+      float thit = -1.0f;
+      const bool hit = mt_ray_triangle_test(f3(c), f3(c + 3), f3(c + 6), r, &thit);
+      o[0] = hit ? 1.0f : 0.0f, o[1] = thit;
+    } else if (op == 2) {
+      Ray r;
+      r.make_ray(f3(c), f3(c + 4), c[3], c[7]);
+      float4x4 m;
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) m.m[i][j] = c[8 + 4 * i + j];
+      float mult = 0.0f;
+      const Ray t = make_transformed_ray(r, m, &mult);
+      const float3 to = t.get_origin(), td = t.get_direction();
+      const float v[9] = {to.x, to.y, to.z, td.x, td.y, td.z, t.get_tmin(), t.get_tmax(), mult};
+      for (int i = 0; i < 9; ++i) o[i] = v[i];
+    } else {
+      const float3 b = Barycentric(f3(c), f3(c + 3), f3(c + 6), f3(c + 9));
+      o[0] = b.x, o[1] = b.y, o[2] = b.z;
+    }
+  }
+  return 0;
+}
+
 // One node decoded by the oracle's decoders, in the record layout of
 // oracle/ref_pin/pin_decoders.cpp (which decodes with the reference header).
 int oracle_decode_node(const uint8_t* blob, uint32_t unit, int kind, double* out) {

@@ -7,9 +7,12 @@
  * compiled here (it needs Mesa, the Vulkan SDK, Boost, flex and bison), and it
  * ships no tests or golden vectors for this path.  The node decoders,
  * set_child_bounds and float4x4 product are pinned against the reference's own
- * header compiled with a stub (oracle/ref_pin/); the traversal, treelet
- * partition and prefetch decision are restated line by line and checked
- * against hand-derived known answers only: parity unpinned for those parts.
+ * header compiled with a stub, and the ray geometry (calculate_idir,
+ * ray_box_test, mt_ray_triangle_test, make_transformed_ray, Barycentric and
+ * the vector operators) against the reference's own functions compiled in
+ * place (oracle/ref_pin/); the traversal, treelet partition and prefetch
+ * decision are restated line by line and checked against hand-derived known
+ * answers only: parity unpinned for those parts.
  */
 #ifndef ORACLE_RT_H
 #define ORACLE_RT_H
@@ -28,6 +31,12 @@ typedef struct oracle_treelets oracle_treelets;
  * oracle/ref_pin/pin_decoders.cpp, which decodes with the reference's own
  * vulkan_acceleration_structure_util.h.  Returns 0 or -1. */
 int oracle_decode_node(const uint8_t* blob, uint32_t unit, int kind, double* out);
+
+/* The oracle's ray geometry on n cases (op 0 calculate_idir + ray_box_test,
+ * 1 mt_ray_triangle_test, 2 make_transformed_ray, 3 Barycentric), in the case
+ * and result layouts of oracle/ref_pin/pin_geometry.cpp, which runs the
+ * reference's own functions.  Returns 0 or -1. */
+int oracle_geometry(int op, const float* in, uint32_t n, float* out);
 
 /* createTreelets + buildNodeToRootMap over a blob (vulkan_ray_tracing.cc:823-1470,
  * :475-489).  Returns NULL on a condition where the reference asserts; the

@@ -47,3 +47,37 @@ def test_library_blobs_walk_like_the_reference(built):
         assert len(quads) and (quads[:, 2 + 6] == 0).all() and (quads[:, 2 + 3] == 0).all()
         internal = recs[recs[:, 0] == 1]
         assert ((internal[:, 1] + internal[:, 2 + 3]) < n_units).all()
+
+
+GEOMETRY = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "geometry.npz")
+
+
+@pytest.mark.parametrize("op,name", [(0, "box"), (1, "tri"), (2, "xform"), (3, "bary")])
+def test_oracle_geometry_matches_reference_functions(op, name):
+    """The oracle's calculate_idir + ray_box_test, mt_ray_triangle_test,
+    make_transformed_ray and Barycentric against the reference's own
+    functions (vulkan_ray_tracing.cc:148-257, :3089-3130, compiled in place by
+    oracle/ref_pin; fixtures made by tests/golden/make_geometry_golden.py) on
+    seeded cases with signed zeros, clamped directions, face origins, flat and
+    inverted boxes, det = 0 rays and degenerate triangles.  Bit-exact; NaN
+    results must be NaN on both sides (their payload is the host's)."""
+    from oracle import oracle as orc
+
+    g = np.load(GEOMETRY)
+    cases, expect = g[f"in_{name}"], g[f"out_{name}"]
+    got = orc.geometry(op, cases)
+    same = (got.view(np.uint32) == expect.view(np.uint32)) | (np.isnan(got) & np.isnan(expect))
+    bad = np.nonzero(~same.all(axis=1))[0]
+    assert len(bad) == 0, (name, bad[:5], got[bad[:2]], expect[bad[:2]])
+
+
+def test_geometry_golden_covers_the_edge_cases():
+    g = np.load(GEOMETRY)
+    box_in, box_out = g["in_box"], g["out_box"]
+    d = box_in[:, 9:12]
+    assert (np.signbit(d) & (d == 0)).any() and (~np.signbit(d) & (d == 0)).any()  # both zero signs
+    assert (np.abs(d[d != 0]) < 2.0 ** -80).any()                                  # clamped components
+    assert box_out[:, 3].sum() > 500 and (box_out[:, 3] == 0).sum() > 500           # hits and misses
+    tri_out = g["out_tri"]
+    assert ((tri_out[:, 0] == 1) & np.isnan(tri_out[:, 1])).sum() > 50             # det = 0 "hits" with NaN t
+    assert ((tri_out[:, 0] == 1) & np.isfinite(tri_out[:, 1])).sum() > 400
