@@ -9,10 +9,11 @@
  * set_child_bounds and float4x4 product are pinned against the reference's own
  * header compiled with a stub, and the ray geometry (calculate_idir,
  * ray_box_test, mt_ray_triangle_test, make_transformed_ray, Barycentric and
- * the vector operators) against the reference's own functions compiled in
- * place (oracle/ref_pin/); the traversal, treelet partition and prefetch
- * decision are restated line by line and checked against hand-derived known
- * answers only: parity unpinned for those parts.
+ * the vector operators) and the treelet partition (createTreelets,
+ * buildNodeToRootMap, remapBVHToTreeletLayout) against the reference's own
+ * functions compiled in place (oracle/ref_pin/); the traversal and the
+ * prefetch decision are restated line by line and checked against
+ * hand-derived known answers only: parity unpinned for those parts.
  */
 #ifndef ORACLE_RT_H
 #define ORACLE_RT_H

@@ -81,3 +81,59 @@ def test_geometry_golden_covers_the_edge_cases():
     tri_out = g["out_tri"]
     assert ((tri_out[:, 0] == 1) & np.isnan(tri_out[:, 1])).sum() > 50             # det = 0 "hits" with NaN t
     assert ((tri_out[:, 0] == 1) & np.isfinite(tri_out[:, 1])).sum() > 400
+
+
+TREELETS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "treelets.npz")
+
+
+def _treelet_cases():
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_treelet_golden import CASES
+
+    return [(name, kind, n, seed, b) for name, kind, n, seed, budgets in CASES for b in budgets]
+
+
+@pytest.mark.parametrize("name,kind,n_tris,seed,budget", _treelet_cases())
+def test_partition_matches_reference_create_treelets(built, name, kind, n_tris, seed, budget):
+    """The oracle's and the library's treelet partitions against the
+    reference's own createTreelets / buildNodeToRootMap /
+    remapBVHToTreeletLayout (vulkan_ray_tracing.cc:456-510, :823-1509,
+    compiled in place by oracle/ref_pin; fixtures made by
+    tests/golden/make_treelet_golden.py): roots, member lists in order, the
+    node->root map, metadata indices and the remapped layout, or the remap's
+    assert where the reference asserts."""
+    import hashlib
+    import sys
+
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_treelet_golden import STRIDE, blob_of
+
+    g = np.load(TREELETS)
+    blob = blob_of(kind, n_tris, seed)
+    assert hashlib.sha256(blob.tobytes()).digest() == g[f"{name}__sha256"].tobytes(), "scene generator changed"
+    key = f"{name}__{budget}__"
+    roots, first, members = g[key + "roots"], g[key + "member_first"], g[key + "members"]
+    tl = orc.Treelets(blob, budget)
+    for d in (tl.get(), rt.Partition(rt.Blob.wrap(blob), budget).get()):
+        assert np.array_equal(d["roots"].astype(np.uint64), roots)
+        assert np.array_equal(d["member_first"].astype(np.uint64), first)
+        assert np.array_equal(d["members"].astype(np.uint64), members)
+        node_root = d["node_root"].astype(np.uint64)
+        nm = g[key + "node_map"]
+        assert np.array_equal(node_root[nm[:, 0].astype(np.int64)], nm[:, 1])
+        assert int((d["node_root"] != 0xFFFFFFFF).sum()) == len(nm)
+    meta = g[key + "meta"]  # metadata index = rank of the root in address order
+    assert np.array_equal(meta[:, 0], roots) and np.array_equal(meta[:, 1], np.arange(len(roots), dtype=np.uint64))
+    if bool(g[key + "remap_asserts"]):
+        with pytest.raises(orc.OracleError, match="remapBVHToTreeletLayout asserts"):
+            tl.remap(stride=STRIDE)
+    else:
+        m = tl.remap(stride=STRIDE)
+        rm = g[key + "remap"]
+        assert np.array_equal(m[rm[:, 0].astype(np.int64)], rm[:, 1])
+        assert int((m != np.uint64(0xFFFFFFFFFFFFFFFF)).sum()) == len(rm)
