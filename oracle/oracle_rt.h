@@ -4,16 +4,15 @@
  * links or calls it.
  *
  * Parity status: the reference (Vulkan-Sim's vulkan_ray_tracing.cc) cannot be
- * compiled here (it needs Mesa, the Vulkan SDK, Boost, flex and bison), and it
- * ships no tests or golden vectors for this path.  The node decoders,
- * set_child_bounds and float4x4 product are pinned against the reference's own
- * header compiled with a stub, and the ray geometry (calculate_idir,
- * ray_box_test, mt_ray_triangle_test, make_transformed_ray, Barycentric and
- * the vector operators) and the treelet partition (createTreelets,
- * buildNodeToRootMap, remapBVHToTreeletLayout) against the reference's own
- * functions compiled in place (oracle/ref_pin/); the traversal and the
- * prefetch decision are restated line by line and checked against
- * hand-derived known answers only: parity unpinned for those parts.
+ * built as a whole here (it needs Mesa, the Vulkan SDK, Boost, flex and bison),
+ * and it ships no tests or golden vectors for this path.  The path's own
+ * functions are compiled in place from the reference tree by oracle/ref_pin/
+ * (the decoder header unmodified; the geometry, createTreelets /
+ * buildNodeToRootMap / remapBVHToTreeletLayout, traceRay and
+ * traceRayWithTreelets as extracted line ranges), and the oracle is pinned
+ * against their outputs (tests/golden/).  The RT unit's prefetch decision
+ * (shader.cc) needs the cycle simulator: it is restated and checked against
+ * hand-derived known answers only, parity unpinned for that part.
  */
 #ifndef ORACLE_RT_H
 #define ORACLE_RT_H

@@ -67,3 +67,33 @@ def edge_rays() -> np.ndarray:
     add([0.25, 0.0, 0.25], [0.0, 1.0, 0.0])        # on the ground plane
     add([0.5, 0.5, -1.5], [3.0, 4.0, 12.0])        # unnormalised
     return np.concatenate(rs)
+
+
+TX_SIZE = (64, 64, 128, 8, 64, 64, 64)  # bytes per transaction type (STRUCTURE .. PROCEDURAL_LEAF)
+
+
+def reference_words(hits, visits, treelets, walk: int) -> list:
+    """Per-ray result words in the layout of oracle/ref_pin/pin_traversal.cpp
+    (hit_geometry, geometry_index, primitive_index, instance_index,
+    world_min_thit, barycentric, intersection_point, then per transaction its
+    unit, type, size and treelet root; zeros for a ray with no hit), built from
+    a trace's hit records and visit / treelet-id traces."""
+    out = []
+    for k in range(len(hits)):
+        h = hits[k]
+        n = int(h["n_visits"])
+        assert n <= visits.shape[1], "trace capacity too small for the golden comparison"
+        w = np.zeros(12 + 4 * n, np.uint32)
+        if h["hit_geometry"]:
+            w[0:4] = (1, h["geometry_index"], h["primitive_index"], h["instance_index"])
+            w[4:11] = np.concatenate([[h["world_min_thit"]], h["barycentric"], h["intersection_point"]]).astype(
+                np.float32).view(np.uint32)
+        w[11] = n
+        v = visits[k, :n].astype(np.uint32)
+        tx = w[12:].reshape(n, 4)
+        tx[:, 0] = v >> 3
+        tx[:, 1] = v & 7
+        tx[:, 2] = np.array(TX_SIZE, np.uint32)[v & 7]
+        tx[:, 3] = treelets[k, :n] if walk == 1 else 0xFFFFFFFF
+        out.append(w)
+    return out

@@ -137,3 +137,59 @@ def test_partition_matches_reference_create_treelets(built, name, kind, n_tris, 
         rm = g[key + "remap"]
         assert np.array_equal(m[rm[:, 0].astype(np.int64)], rm[:, 1])
         assert int((m != np.uint64(0xFFFFFFFFFFFFFFFF)).sum()) == len(rm)
+
+
+TRAVERSAL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "traversal.npz")
+
+
+def _traversal_cases():
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_traversal_golden import CASES
+
+    return CASES
+
+
+def traversal_case_inputs(case, sname, rname):
+    """The scene and rays of one golden traversal case, regenerated and
+    checked against the digests the fixture recorded."""
+    import hashlib
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_traversal_golden import rays_of, scene
+
+    g = np.load(TRAVERSAL)
+    blob, rays = scene(sname), rays_of(rname)
+    assert hashlib.sha256(blob.tobytes()).digest() == g[f"scene__{sname}__sha256"].tobytes(), "scene changed"
+    assert hashlib.sha256(rays.tobytes()).digest() == g[f"rays__{rname}__sha256"].tobytes(), "rays changed"
+    return blob, rays, g
+
+
+@pytest.mark.parametrize("case,sname,rname,walk,flags,budget,offset", _traversal_cases())
+def test_oracle_traversal_matches_reference_walks(built, case, sname, rname, walk, flags, budget, offset):
+    """The oracle's traceRay / traceRayWithTreelets restatement against the
+    reference's own walks (vulkan_ray_tracing.cc:1522-3076, compiled in place
+    by oracle/ref_pin; fixtures made by tests/golden/make_traversal_golden.py):
+    hit records bit for bit, every transaction's unit, type and size in order,
+    and each transaction's treelet in the treelet walk."""
+    import sys
+
+    from helpers import reference_words
+    from oracle import oracle as orc
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_traversal_golden import digest
+
+    blob, rays, g = traversal_case_inputs(case, sname, rname)
+    tl = orc.Treelets(blob, budget) if walk else None
+    mode = 0 if walk == 0 else (2 if offset else 1)
+    hits, vis, tids = orc.trace(blob, rays, mode, tl, default_flags=flags, capacity=1024, want_visits=True,
+                                want_treelets=walk == 1)
+    words = reference_words(hits, vis, tids, walk)
+    got = np.stack([digest(w) for w in words])
+    bad = np.nonzero((got != g[f"{case}__digests"]).any(axis=1))[0]
+    assert len(bad) == 0, (case, "rays differing from the reference:", bad[:10])
+    if f"{case}__words" in g.files:
+        assert np.array_equal(np.concatenate(words), g[f"{case}__words"])

@@ -2,6 +2,8 @@
 treelet-access traces must be bit-identical (the kernels keep the reference's
 FP32 operation order with FMA contraction off, so hit t is compared bit for
 bit, no tolerance)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -312,3 +314,47 @@ def test_device_offset_walk(ctx):
             assert_traces_equal(vis, ov, oh["n_visits"], f"{name} visits, device offset")
             assert_traces_equal(tids, ot, oh["n_visits"], f"{name} treelet ids, device offset")
         scene.close()
+
+
+def _golden_traversal_cases():
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_traversal_golden import CASES
+
+    return CASES
+
+
+@pytest.mark.parametrize("case,sname,rname,walk,flags,budget,offset", _golden_traversal_cases())
+def test_walks_match_reference_golden(ctx, case, sname, rname, walk, flags, budget, offset):
+    """The GPU walks against the reference's own traceRay /
+    traceRayWithTreelets (golden digests from tests/golden/traversal.npz, made
+    by running the reference's code): traceRay's cases in the plain walk,
+    traceRayWithTreelets's in the treelet-order and staged walks, with the
+    reference's nonzero device_offset where the case has one.  Hit records,
+    transactions and treelet ids bit for bit."""
+    import sys
+
+    from helpers import reference_words
+    from test_golden import traversal_case_inputs
+
+    import treelet_rt as rt
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_traversal_golden import digest
+
+    blob, rays, g = traversal_case_inputs(case, sname, rname)
+    scene = rt.Scene(ctx, rt.Blob.wrap(blob))
+    scene.form_treelets(budget)
+    if offset:
+        scene.set_device_offset(offset)
+    modes = (rt.MODE_PLAIN,) if walk == 0 else (rt.MODE_TREELET, rt.MODE_STAGED)
+    want = g[f"{case}__digests"]
+    for mode in modes:
+        hits, vis, tids = scene.trace_host(rays, mode, default_flags=flags, capacity=1024, want_visits=True,
+                                           want_treelets=True)
+        got = np.stack([digest(w) for w in reference_words(hits, vis, tids, walk)])
+        bad = np.nonzero((got != want).any(axis=1))[0]
+        assert len(bad) == 0, (case, mode, "rays differing from the reference:", bad[:10])
+    scene.close()
