@@ -12,8 +12,9 @@ treelets of 8 KiB.  A step traces the primary batch, then the bounce batch.
 Prints one JSON line.  `value` is the treelet-staged traversal with rays and
 hits resident in HBM; `e2e` goes through the C ABI with host buffers
 (rt_trace_host: host-to-device copy of the rays, device-to-host copy of the
-hits inside the timed region).  `--impl reference` times the CPU
-restatement of the reference's traceRay on the host cores instead.
+hits inside the timed region).  `--impl reference` times the reference's own
+traceRay on the host cores instead (compiled in place from its sources into
+oracle/_ref/pin_traversal; the oracle's restatement where that is not built).
 """
 from __future__ import annotations
 
@@ -62,6 +63,39 @@ STAGED_DRAM_BYTES_PER_RAY = {"primary": (118.069248e6 + 45.421056e6) / 262144,
 def _traffic_per_ray():
     """DRAM bytes per ray of the staged kernel, averaged over the primary and bounce launches."""
     return {"staged_dram_bytes_per_ray": (STAGED_DRAM_BYTES_PER_RAY["primary"] + STAGED_DRAM_BYTES_PER_RAY["bounce"]) / 2}
+
+
+REF_WALK = os.path.join(REPO, "oracle", "_ref", "pin_traversal")
+
+
+def cpu_walk_seconds(bb: np.ndarray, rays: np.ndarray, threads: int, reps: int):
+    """Seconds per pass of the CPU baseline over `rays` (plain traceRay order,
+    opaque closest hit) on `threads` host threads, `reps` timed passes after
+    an untimed one.  The reference's own traceRay, compiled in place from its
+    sources (oracle/_ref/pin_traversal), when it is built; else the oracle's
+    restatement.  Returns (seconds per pass, kind)."""
+    if os.path.exists(REF_WALK):
+        import tempfile
+
+        with tempfile.TemporaryDirectory() as d:
+            bp, rp = os.path.join(d, "blob"), os.path.join(d, "rays")
+            bb.tofile(bp)
+            np.ascontiguousarray(rays).tofile(rp)
+            r = subprocess.run([REF_WALK, "--time", bp, rp, "0", "1", str(BUDGET), str(threads), str(reps)],
+                               capture_output=True, text=True, timeout=900)
+        secs = [float(ln.split()[2]) for ln in r.stderr.splitlines() if ln.startswith("rep ")]
+        if r.returncode == 0 and len(secs) == reps:
+            return secs, "reference"
+        print(f"reference walk harness failed ({r.returncode}); timing the oracle port", file=sys.stderr)
+    from oracle import oracle as orc
+
+    orc.trace(bb, rays[: min(len(rays), 2048)], 0, threads=threads)
+    secs = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        orc.trace(bb, rays, 0, threads=threads)
+        secs.append(time.perf_counter() - t)
+    return secs, "port"
 
 
 class ClockSampler:
@@ -147,8 +181,10 @@ def make_workload(ctx_needed: bool = True):
 
 
 def run_reference(args, rank: int, world: int) -> None:
-    """CPU restatement of the reference's traceRay on the host cores: a
-    bounded sample of the same workload per step."""
+    """The reference's CPU traceRay on the host cores, all threads, over a
+    bounded sample of the same workload per step: the reference's own code
+    compiled in place from its sources (oracle/_ref/pin_traversal) when it is
+    built, else the oracle's line-by-line restatement."""
     import treelet_rt as rt
     from oracle import oracle as orc
 
@@ -158,27 +194,20 @@ def run_reference(args, rank: int, world: int) -> None:
     bb = blob.bytes()
     threads = os.cpu_count() or 1
     n_prim = len(prim)
-    sample = args.ref_sample
-    idx = np.linspace(0, n_prim - 1, sample // 2).astype(np.int64)
+    idx = np.linspace(0, n_prim - 1, args.ref_step_rays // 2).astype(np.int64)
     ps = prim[idx]
     ph, _, _ = orc.trace(bb, ps, 0, threads=threads)
     bounce = rt.bounce_rays_host(blob, ps, ph, seed=SEED + 100)
     rays = np.concatenate([ps, bounce])
-    for _ in range(args.warmup):
-        orc.trace(bb, rays[: min(len(rays), 2048)], 0, threads=threads)
-    times = []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        orc.trace(bb, rays, 0, threads=threads)
-        times.append(time.perf_counter() - t)
-    total = sum(times)
+    secs, kind = cpu_walk_seconds(bb, rays, threads, args.steps)
+    total = sum(secs)
     v = len(rays) * args.steps / total / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample_rays_per_step": int(len(rays)), "mode": "traceRay (plain)"},
-        "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": kind,
                          "sample": f"{len(rays)} rays per step: {len(ps)} primary rays spread over the frame + "
                                    f"their {len(bounce)} bounce rays"},
         "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -330,19 +359,15 @@ def run_gpu(args, rank: int, world: int) -> None:
     e2e = n_rays / (sum(e2e_t) / len(e2e_t)) / 1e6 * world
 
     # CPU baseline: oracle traceRay on a bounded sample, all host threads
+    # CPU baseline: the reference's traceRay on a bounded sample, all host threads
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        from oracle import oracle as orc
-
         threads = os.cpu_count() or 1
         idx = np.linspace(0, n_prim - 1, args.ref_sample // 2).astype(np.int64)
-        bb = blob.bytes()
         hb = np.frombuffer(d_bounce.cpu().numpy().tobytes(), rt.RAY_DTYPE)
         sample = np.concatenate([prim[idx], hb[idx]])
-        t = time.perf_counter()
-        orc.trace(bb, sample, 0, threads=threads)
-        dt = time.perf_counter() - t
-        cpu = {"value": round(len(sample) / dt / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+        secs, kind = cpu_walk_seconds(blob.bytes(), sample, threads, 1)
+        cpu = {"value": round(len(sample) / secs[0] / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": kind,
                "sample": f"{len(sample)} rays: {len(idx)} primary rays spread over the frame + their bounce rays"}
 
     if rank == 0:
@@ -737,7 +762,8 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ref-sample", type=int, default=1000000)
+    ap.add_argument("--ref-sample", type=int, default=1000000, help="rays of the CPU-baseline sample")
+    ap.add_argument("--ref-step-rays", type=int, default=262144, help="rays per step of --impl reference")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="small: the same scene with 512x512x1 primary rays + bounces (profiling case)")

@@ -24,8 +24,13 @@
 // intersection_point x y z (floats as bits), n transactions, then per
 // transaction: (address - blob - device offset) / 64, type, size, treelet
 // (root unit of addrToTreeletID(address), or 0xFFFFFFFF in traceRay).
+//
+// Timing: pin_traversal --time <blob> <rays> <mode> <ray flags> <treelet bytes>
+//                              <threads> <reps>   (see time_walk)
 #include <algorithm>
+#include <atomic>
 #include <cassert>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -37,6 +42,7 @@
 #include <list>
 #include <map>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 #include <vector_types.h>
@@ -124,13 +130,16 @@ warp_intersection_table* g_table_row[1] = {&g_table};
 warp_intersection_table** g_table_grid[1] = {g_table_row};
 
 namespace pin {
+// Statistics the walks update.  Atomic so that the timing mode can run the
+// walks on several threads; the world bounds are set by the first ray, which
+// the timing mode traces alone before any thread starts.
 struct FuncSim {
-  unsigned long long g_n_anyhit_rays = 0, g_n_closesthit_rays = 0;
-  unsigned long long g_rt_mem_access_type[16] = {};
-  bool g_rt_world_set = false;
+  std::atomic<unsigned long long> g_n_anyhit_rays{0}, g_n_closesthit_rays{0};
+  std::atomic<unsigned long long> g_rt_mem_access_type[16] = {};
+  std::atomic<bool> g_rt_world_set{false};
   float3 g_rt_world_min{}, g_rt_world_max{};
-  unsigned long long g_max_nodes_per_ray = 0, g_tot_nodes_per_ray = 0, g_max_tree_depth = 0;
-  unsigned long long g_rt_num_hits = 0, g_rt_num_any_hits = 0;
+  std::atomic<unsigned long long> g_max_nodes_per_ray{0}, g_tot_nodes_per_ray{0}, g_max_tree_depth{0};
+  std::atomic<unsigned long long> g_rt_num_hits{0}, g_rt_num_any_hits{0};
 };
 struct ShaderConfig {
   bool remap_to_treelet_layout = false;
@@ -169,7 +178,6 @@ Sim g_sim{&g_gpu};
 FuncSim g_func;
 Context g_ctx{&g_sim, &g_func};
 uint8_t* g_layout_base = reinterpret_cast<uint8_t*>(uintptr_t(1) << 40);
-std::vector<uint8_t> g_alloc;  // gpgpusim_alloc's memory: never read back
 }  // namespace pin
 
 typedef pin::Context gpgpu_context;
@@ -197,7 +205,7 @@ struct VulkanRayTracing {
   static uint8_t* treelet_layout_bvh;
   static void* treelet_metadata;
   static unsigned per_treelet_metadata_size;
-  static unsigned accessedDataSize;
+  static std::atomic<unsigned> accessedDataSize;
 
   static bool isTreeletRoot(StackEntry node);
   static bool isTreeletRoot(uint8_t* addr);
@@ -210,10 +218,9 @@ struct VulkanRayTracing {
   static void remapBVHToTreeletLayout();
   static bool mt_ray_triangle_test(float3 p0, float3 p1, float3 p2, Ray ray_properties, float* thit);
   static float3 Barycentric(float3 p, float3 a, float3 b, float3 c);
-  static void* gpgpusim_alloc(size_t size) {
-    pin::g_alloc.resize(pin::g_alloc.size() + size);
-    return nullptr;
-  }
+  // simulated device memory for the records the walk writes; the memory
+  // space above keeps the bytes, so no address is needed
+  static void* gpgpusim_alloc(size_t) { return nullptr; }
   static void dump_AS(DESCRIPTOR_SET_STRUCT*, VkAccelerationStructureKHR) { abort(); }
   static void traceRayWithTreelets(VkAccelerationStructureKHR _topLevelAS, uint rayFlags, uint cullMask,
                                    uint sbtRecordOffset, uint sbtRecordStride, uint missIndex, float3 origin,
@@ -242,10 +249,11 @@ std::map<uint8_t*, unsigned> VulkanRayTracing::treelet_addr_to_metadata_idx;
 uint8_t* VulkanRayTracing::treelet_layout_bvh = nullptr;
 void* VulkanRayTracing::treelet_metadata = nullptr;
 unsigned VulkanRayTracing::per_treelet_metadata_size = 0;
-unsigned VulkanRayTracing::accessedDataSize = 0;
+std::atomic<unsigned> VulkanRayTracing::accessedDataSize{0};
 
-// the file-scope state of vulkan_ray_tracing.cc the walks read and write
-unsigned rayCount = 0;
+// the file-scope state of vulkan_ray_tracing.cc the walks read and write (the
+// ray counter per thread: it only numbers rays)
+thread_local unsigned rayCount = 0;
 bool use_external_launcher = false;
 const bool dump_trace = false;
 bool treeletsFormed = false;
@@ -300,7 +308,57 @@ uint32_t bits(float f) {
 
 }  // namespace
 
+// Timing mode: the reference's own walk over the rays on `threads` host
+// threads (contiguous ray ranges), `reps` times after one untimed pass; prints
+// "rep <i> <seconds>" per pass on stderr.  The first ray is traced alone
+// first, so that the walk's lazy one-time set-up (createTreelets, the world
+// bounds) is done before the threads start.
+int time_walk(int mode, uint32_t flags, const std::vector<uint8_t>& rays, int threads, int reps) {
+  uint8_t* tlas = g_blob.data();
+  const size_t n = rays.size() / 32;
+  auto trace_range = [&](size_t lo, size_t hi) {
+    for (size_t r = lo; r < hi; ++r) {
+      float v[8];
+      memcpy(v, rays.data() + 32 * r, 32);
+      ptx_thread_info thread;
+      const float3 o = {v[0], v[1], v[2]}, d = {v[4], v[5], v[6]};
+      if (mode == 0)
+        VulkanRayTracing::traceRay(tlas, flags, 0xFF, 0, 0, 0, o, v[3], d, v[7], 0, nullptr, &thread);
+      else
+        VulkanRayTracing::traceRayWithTreelets(tlas, flags, 0xFF, 0, 0, 0, o, v[3], d, v[7], 0, nullptr, &thread);
+    }
+  };
+  trace_range(0, std::min<size_t>(1, n));
+  for (int rep = -1; rep < reps; ++rep) {
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+      pool.emplace_back(trace_range, n * t / threads, n * (t + 1) / threads);
+    for (auto& th : pool) th.join();
+    const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rep >= 0) fprintf(stderr, "rep %d %.6f\n", rep, s);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 9 && std::string(argv[1]) == "--time") {
+    // pin_traversal --time <blob> <rays> <mode> <ray flags> <treelet bytes> <threads> <reps>
+    g_blob = read_file(argv[2]);
+    const std::vector<uint8_t> rays = read_file(argv[3]);
+    const int mode = atoi(argv[4]);
+    pin::g_gpu.cfg.max_treelet_size = strtoull(argv[6], nullptr, 10);
+    const int threads = atoi(argv[7]), reps = atoi(argv[8]);
+    if (g_blob.empty() || rays.empty() || rays.size() % 32 || (mode != 0 && mode != 1) || threads < 1 || reps < 1)
+      return 2;
+    VulkanRayTracing::tlas_addr = g_blob.data();
+    GEN_RT_BVH top;
+    GEN_RT_BVH_unpack(&top, g_blob.data());
+    find_blases(top.RootNodeOffset, 0);
+    if (!freopen("/dev/null", "w", stdout)) return 2;
+    std::cout.setstate(std::ios::failbit);
+    return time_walk(mode, (uint32_t)strtoul(argv[5], nullptr, 10), rays, threads, reps);
+  }
   if (argc != 8) {
     fprintf(stderr, "usage: pin_traversal <blob> <rays> <mode 0|1> <ray flags> <treelet bytes> <device offset> <out>\n");
     return 2;

@@ -96,12 +96,18 @@ def build_oracle(verbose: bool = False, force: bool = False) -> str:
 
 
 def build_reference_pin(verbose: bool = False) -> None:
-    """Builds oracle/_ref/pin_decoders from the reference's own decoder header
-    when the reference tree is present (it is not on every machine)."""
+    """Builds the checker harnesses of oracle/ref_pin (the reference's own
+    decoders, geometry, treelet formation and walks, compiled in place) into
+    oracle/_ref/ when the reference tree is present.  Elsewhere, when the
+    extracted reference files came along in oracle/_ref/extract/, rebuilds
+    the walk harness from them (the CPU baseline times it); otherwise there is
+    nothing to build."""
     ref = os.environ.get("TREELET_RT_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src", "cuda-sim")):
-        return
-    _run(["make", "-s", "-C", os.path.join(ORACLE_DIR, "ref_pin"), f"REFERENCE={ref}"], verbose)
+    pin = os.path.join(ORACLE_DIR, "ref_pin")
+    if os.path.isdir(os.path.join(ref, "src", "cuda-sim")):
+        _run(["make", "-s", "-C", pin, f"REFERENCE={ref}"], verbose)
+    elif os.path.exists(os.path.join(ORACLE_DIR, "_ref", "extract", "tr_walks.inc")):
+        _run(["make", "-s", "-C", pin, "extracted"], verbose)
 
 
 def build_all(verbose: bool = False, force: bool = False) -> None:
