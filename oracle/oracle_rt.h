@@ -10,9 +10,10 @@
  * (the decoder header unmodified; the geometry, createTreelets /
  * buildNodeToRootMap / remapBVHToTreeletLayout, traceRay and
  * traceRayWithTreelets as extracted line ranges), and the oracle is pinned
- * against their outputs (tests/golden/).  The RT unit's prefetch decision
- * (shader.cc) needs the cycle simulator: it is restated and checked against
- * hand-derived known answers only, parity unpinned for that part.
+ * against their outputs (tests/golden/), as is its RT-unit prefetch decision
+ * (the decision block of shader.cc's rt_unit::cycle, extracted and compiled
+ * in a stand-in RT unit).  The RT-unit replay's memory model is this
+ * project's own: no reference code pins it.
  */
 #ifndef ORACLE_RT_H
 #define ORACLE_RT_H

@@ -193,3 +193,70 @@ def test_oracle_traversal_matches_reference_walks(built, case, sname, rname, wal
     assert len(bad) == 0, (case, "rays differing from the reference:", bad[:10])
     if f"{case}__words" in g.files:
         assert np.array_equal(np.concatenate(words), g[f"{case}__words"])
+
+
+PREFETCH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "prefetch.npz")
+
+
+def _prefetch_scenes():
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_prefetch_golden import SCENES
+
+    return SCENES
+
+
+@pytest.mark.parametrize("name,budget,n_cases,seed", _prefetch_scenes())
+def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases, seed):
+    """The oracle's treelet-prefetch decision against the reference's own
+    decision block (shader.cc:3419-3685, compiled in place by oracle/ref_pin;
+    fixtures made by tests/golden/make_prefetch_golden.py): for every case the
+    32-byte chunks queued (address and node, in order, for the most popular
+    treelet and for the second-prefetch rule) and the carried state after the
+    decision."""
+    import hashlib
+    import sys
+
+    from oracle import oracle as orc
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_prefetch_golden import NONE, case_list, case_words, digest, scene
+
+    g = np.load(PREFETCH)
+    blob = scene(name)
+    assert hashlib.sha256(blob.tobytes()).digest() == g[f"{name}__scene_sha256"].tobytes(), "scene changed"
+    cases = case_list(blob, budget, n_cases, seed)
+    assert hashlib.sha256(case_words(cases).tobytes()).digest() == g[f"{name}__cases_sha256"].tobytes()
+    tl = orc.Treelets(blob, budget)
+    d = tl.get()
+    first = d["member_first"].astype(np.int64)
+    index = {int(r): k for k, r in enumerate(d["roots"])}
+
+    def chunks(root, j0, j1):
+        k = index[root]
+        out = []
+        for m, size in zip(d["members"][first[k] + j0:first[k] + j1], d["member_bytes"][first[k] + j0:first[k] + j1]):
+            out += [(int(m) * 64 + 32 * c, int(m)) for c in range((int(size) + 31) // 32)]
+        return out
+
+    bad = []
+    for i, c in enumerate(cases):
+        state = np.zeros(1, orc.STATE_DTYPE)[0]
+        state["last_prefetched"], state["last_prefetched_second"] = c["last_prefetched"], c["last_second"]
+        state["last_rejected"], state["queue_len"] = c["last_rejected"], c["queue_len"]
+        dec, st = orc.prefetch_decide(tl, c["next_unit"], heuristic=c["heuristic"], max_queue=c["max_queue"],
+                                      threshold=c["threshold"], second_prefetch=bool(c["second"]), state=state)
+        queued = []
+        if dec["submitted"]:
+            queued += chunks(int(dec["treelet"]), int(dec["first_member"]),
+                             int(dec["first_member"]) + int(dec["n_members"]))
+        if dec["second_treelet"] != NONE:
+            queued += chunks(int(dec["second_treelet"]), 0, int(first[index[int(dec["second_treelet"])] + 1]
+                                                                 - first[index[int(dec["second_treelet"])]]))
+        words = [len(queued)] + [x for pair in queued for x in pair] + [
+            int(st["last_prefetched"]), int(st["last_prefetched_second"]), int(st["last_rejected"]),
+            int(st["queue_len"])]
+        if not np.array_equal(digest(np.array(words, np.uint64)), g[f"{name}__digests"][i]):
+            bad.append(i)
+    assert not bad, (name, "cases differing from the reference:", bad[:10])
