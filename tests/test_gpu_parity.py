@@ -275,6 +275,49 @@ def test_host_trace_chunks_match_device_trace(ctx, n):
     scene.close()
 
 
+def test_host_trace_into_pinned_hits(ctx):
+    """With page-locked hit records rt_trace_host lets the kernel write them
+    straight into host memory (no copy-out, one launch): hits and counters
+    equal a device-side rt_trace, with and without per-ray flags, in every
+    mode, and a pageable buffer still takes the copy path with the same
+    result."""
+    import ctypes as C
+
+    import torch
+
+    import treelet_rt as rt
+    from treelet_rt._ffi import check, lib
+
+    n = 300_000
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 128 * 128, 5)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_TERRAIN_INSTANCES), 600, 500, 1, 6, 1e-4, 1e30)[:n]
+    flags = np.random.default_rng(1).choice(
+        np.array([rt.RAY_FLAG_OPAQUE, rt.RAY_FLAG_OPAQUE | rt.RAY_FLAG_TERMINATE_ON_FIRST_HIT], np.uint32), size=n)
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    h_rays = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8)).pin_memory()
+    h_flags = torch.from_numpy(flags.view(np.uint8)).pin_memory()
+    d_rays, d_flags = h_rays.cuda(), h_flags.cuda()
+    for mode, _, name in _modes():
+        for use_flags in (False, True):
+            d_hits = torch.zeros(n * 64, dtype=torch.uint8, device="cuda")
+            scene.trace(d_rays, d_hits, mode, flags=d_flags if use_flags else None, n=n)
+            torch.cuda.synchronize()
+            dev_stats = scene.stats()
+            ref = d_hits.cpu().numpy().tobytes()
+            pinned = torch.full((n * 64,), 0xAB, dtype=torch.uint8).pin_memory()
+            fp = C.c_void_p(h_flags.data_ptr()) if use_flags else None
+            check(lib().rt_trace_host(scene.handle, C.c_void_p(h_rays.data_ptr()), fp, rt.RAY_FLAG_OPAQUE, n, mode,
+                                      C.c_void_p(pinned.data_ptr()), None))
+            assert pinned.numpy().tobytes() == ref, f"{name}: hits written to page-locked memory differ"
+            host_stats = scene.stats()
+            assert host_stats["node_bytes"] == dev_stats["node_bytes"] > 0, name
+            assert host_stats["device_status"] == 0, name
+        pageable, _, _ = scene.trace_host(rays, mode, flags=flags)
+        assert pageable.tobytes() == ref, f"{name}: copy path differs"
+    scene.close()
+
+
 def test_device_offset_walk(ctx):
     """rt_scene_set_device_offset(nonzero) reproduces the treelet order of the
     reference's nonzero device_offset (oracle mode 2) in the treelet and staged

@@ -135,9 +135,6 @@ struct rt_scene {
 
 namespace {
 
-constexpr int kPlainCap = 96;
-constexpr int kTreeletCap = 96;
-
 rt_status cuda_fail(cudaError_t e, const char* what) {
   return rti::fail(RT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -666,6 +663,18 @@ rt_status trace_launch(rt_scene* s, const rt_ray* rays, const uint32_t* flags, u
   return launch_trace(a, mode, s->tuning, s->slot_bytes, st, keep);
 }
 
+// The device address of a page-locked, mapped host array (cudaHostAlloc or
+// cudaHostRegister with mapping, which unified addressing gives by default),
+// or nullptr for pageable memory.
+void* mapped_host(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // pageable memory on older drivers: not an error here
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 // Waits for every stream of the host path; returns `st` (or the first CUDA
 // error if `st` is RT_OK).
 rt_status host_finish(rt_scene* s, rt_status st) {
@@ -733,6 +742,33 @@ rt_status rt_trace_host(rt_scene* s, const rt_ray* rays, const uint32_t* flags, 
   RT_CUDA(cudaSetDevice(s->ctx->device));
   const uint32_t cap = (trace && (trace->visits || trace->treelets)) ? trace->capacity : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  // Page-locked hit records: the kernel writes them straight into host memory
+  // as rays finish, so no copy-out follows the trace and one launch over all
+  // rays needs no chunks (chunked launches each pay a tail of long rays).
+  // Rays and flags are copied in first, in one copy each.
+  if (!cap) {
+    rt_hit* mapped_hits = static_cast<rt_hit*>(mapped_host(hits));
+    if (mapped_hits) {
+      const size_t b_rays = al(sizeof(rt_ray) * (size_t)n), b_flags = flags ? sizeof(uint32_t) * (size_t)n : 0;
+      if (b_rays + b_flags > s->io_bytes) {
+        cudaFree(s->d_io);
+        s->d_io = nullptr;
+        s->io_bytes = 0;
+        st = dalloc((uint8_t**)&s->d_io, b_rays + b_flags);
+        if (st != RT_OK) return st;
+        s->io_bytes = b_rays + b_flags;
+      }
+      rt_ray* d_rays = (rt_ray*)s->d_io;
+      uint32_t* d_flags = flags ? (uint32_t*)((uint8_t*)s->d_io + b_rays) : nullptr;
+      cudaError_t e = cudaMemcpyAsync(d_rays, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, s->stream);
+      if (e == cudaSuccess && flags)
+        e = cudaMemcpyAsync(d_flags, flags, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, s->stream);
+      if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host"));
+      st = trace_launch(s, d_rays, d_flags, default_flags, n, mode, mapped_hits, nullptr, s->stream, s->d_queue,
+                        false);
+      return host_finish(s, st);
+    }
+  }
   const size_t b_rays = al(sizeof(rt_ray) * (size_t)n), b_flags = flags ? al(sizeof(uint32_t) * (size_t)n) : 0;
   const size_t b_hits = al(sizeof(rt_hit) * (size_t)n);
   const size_t b_vis = (trace && trace->visits) ? al(sizeof(uint32_t) * (size_t)n * cap) : 0;
