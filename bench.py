@@ -56,8 +56,8 @@ def _peaks():
 # the ncu capture summarised in profiles/trace_kernels_terrain_instances.md: the same scene with
 # 262,144 rays per launch (the full launch of 2,097,152 rays is too large to capture with
 # --set full); scaled to a full launch by the ray count.
-STAGED_DRAM_BYTES_PER_RAY = {"primary": (118.069248e6 + 45.421056e6) / 262144,
-                             "bounce": (287.418880e6 + 134.067968e6) / 262144}
+STAGED_DRAM_BYTES_PER_RAY = {"primary": (104.267264e6 + 14.503936e6) / 262144,
+                             "bounce": (169.227520e6 + 30.532608e6) / 262144}
 
 
 def _traffic_per_ray():

@@ -3,9 +3,10 @@ VulkanRayTracing::traceRay and traceRayWithTreelets
 (src/cuda-sim/vulkan_ray_tracing.cc:1522-3076), run by the harness
 oracle/ref_pin/pin_traversal.cpp, on hand-assembled and seeded scenes:
 closest-hit, non-opaque and terminate-on-first-hit rays, primary and bounce
-rays, the edge rays of helpers.edge_rays, treelet budgets from 192 B to 8 KiB,
-shared BLASes, rotated / scaled / translated instances, and a nonzero
-device_offset for the treelet walk.
+rays, ambient-occlusion rays (tmax 0.1, terminate on first hit), the edge rays
+of helpers.edge_rays, treelet budgets from 192 B to 32 KiB, shared BLASes,
+rotated / scaled / translated instances, and a nonzero device_offset for the
+treelet walk.
 
 Each ray's result is serialized as uint32 words, exactly as the harness
 writes it: hit_geometry, geometry_index, primitive_index, instance_index,
@@ -62,6 +63,9 @@ CASES = [
     ("instanced_plain", "instanced", "instanced_mix", 0, 1, 8192, 0),
     ("instanced_treelet_4096", "instanced", "instanced_mix", 1, 1, 4096, 0),
     ("instanced_treelet_4096_terminate", "instanced", "instanced_mix", 1, 5, 4096, 0),
+    ("blobs_ao_plain", "blobs", "blobs_ao", 0, 5, 8192, 0),
+    ("blobs_ao_treelet_4096", "blobs", "blobs_ao", 1, 5, 4096, 0),
+    ("blobs_ao_treelet_32768", "blobs", "blobs_ao", 1, 5, 32768, 0),
 ]
 FULL = ("kat", "coplanar")  # scenes whose full result words are kept
 
@@ -97,6 +101,8 @@ def scene(name):
         return rt.Blob.gen(rt.SCENE_SHARED_BLAS, 512, 4).bytes()
     if name == "instanced":
         return instanced_blob().bytes()
+    if name == "blobs":
+        return rt.Blob.gen(rt.SCENE_BLOBS, 20000, 6).bytes()
     raise KeyError(name)
 
 
@@ -128,6 +134,15 @@ def rays_of(name):
         return _mix(scene("cube"), rt.default_camera(rt.SCENE_CUBE_PLANE), 24, 2)
     if name == "shared_mix":
         return _mix(scene("shared"), rt.default_camera(rt.SCENE_SHARED_BLAS), 16, 3)
+    if name == "blobs_ao":
+        # ambient-occlusion rays: cosine hemisphere at primary hits, tmax 0.1
+        from oracle import oracle as orc
+
+        blob = scene("blobs")
+        prim = rt.camera_rays(rt.default_camera(rt.SCENE_BLOBS), 96, 96, 1, 5, 1e-4, 1e30)
+        ph, _, _ = orc.trace(blob, prim, 0)
+        hit = ph["hit_geometry"] == 1
+        return rt.bounce_rays_host(rt.Blob.wrap(blob), prim[hit], ph[hit], seed=17, tmin=1e-4, tmax=0.1)
     if name == "instanced_mix":
         cam = rt.Camera((0.0, 1.5, -9.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 50.0)
         return _mix(scene("instanced"), cam, 20, 4)
