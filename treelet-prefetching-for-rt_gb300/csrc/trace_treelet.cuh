@@ -25,20 +25,35 @@ constexpr uint32_t kRouteOther = 6, kRouteInst = 12;  // route bits (treelets.h)
 // node and precomputed.  The staged location of a node (dense treelet << 10 |
 // 64-byte slot in that treelet's image) is read from the node table when a
 // warp has a staged slot; pinned nodes are named by their record.
+//
+// Fields a step rarely needs live in the tail of the stack array, in local
+// memory, instead of registers (kColdWords 64-bit words after the 2 CAP stack
+// entries): the world direction, the closest hit, the trace rows and, in the
+// unstaged walk, the world origin and inverse direction, which only TLAS
+// nodes and instance entries read.  Fewer live registers let the treelet
+// walk run four CTAs per SM at 64 registers: +5% on bounce rays, +2% on
+// primary rays; the staged walk, with its pinned-record state, measured best
+// with the world ray in registers at three CTAs per SM.
+constexpr int kColdWords = 9;
+
 template <int CAP, bool STAGED, bool MULTI>
 struct Walker {
-  rtm::V3 O, D, idir;
-  float tmin, tmax, min_thit, c_tobj;
+  static constexpr bool kColdWorld = !STAGED;
+  rtm::V3 O, idir;  // world ray (registers only when !kColdWorld)
+  float tmin, tmax, min_thit;
   bool terminate, fast, ic_fast;  // FAST min/max allowed for the world / object ray
-  uint32_t c_leaf, c_inst, status;
-  unsigned long long* stk;  // 2 * CAP entries, a local array of the kernel
+  uint32_t status;
+  unsigned long long* stk;  // 2 * CAP + kColdWords entries, a local array of the kernel
   int ncu, not_;            // entries on cu and on ot
   // The top of `cu` when it was pushed by the previous node visit: the node
   // the walk pops next, kept in a register instead of a local-memory round
   // trip (0 = none; no stack entry is 0, a blob's unit 0 is its TLAS header).
   unsigned long long nxt;
   InstCtx ic;
-  Recorder rec;
+  // Visit recording: the counts in registers, the trace rows in the cold tail.
+  struct Counts {
+    uint32_t cap, n, bytes;
+  } rec;
   SceneView v;
   uint32_t smem_reads, gmem_reads;
   uint32_t pin_base;  // shared address of the pinned records, 0 = none
@@ -49,6 +64,57 @@ struct Walker {
   __device__ __forceinline__ void clear() {
     nxt = 0;
     ncu = not_ = 0;
+  }
+
+  // ---- the cold tail: stk[2 CAP + k]
+  __device__ __forceinline__ unsigned long long& cold(int k) const { return stk[2 * CAP + k]; }
+  static __device__ __forceinline__ unsigned long long pack(float a, float b) {
+    return (unsigned long long)__float_as_uint(a) | ((unsigned long long)__float_as_uint(b) << 32);
+  }
+  static __device__ __forceinline__ float lo(unsigned long long w) { return __uint_as_float((uint32_t)w); }
+  static __device__ __forceinline__ float hi(unsigned long long w) { return __uint_as_float((uint32_t)(w >> 32)); }
+  __device__ __forceinline__ void set_dir(rtm::V3 d) {
+    cold(0) = pack(d.x, d.y);
+    cold(1) = pack(d.z, 0.0f);
+  }
+  __device__ __forceinline__ rtm::V3 dir() const {
+    const unsigned long long a = cold(0), b = cold(1);
+    return rtm::v3(lo(a), hi(a), lo(b));
+  }
+  __device__ __forceinline__ void set_hit(uint32_t leaf, uint32_t inst, float tobj) {
+    cold(2) = (unsigned long long)leaf | ((unsigned long long)inst << 32);
+    cold(3) = pack(tobj, 0.0f);
+  }
+  __device__ __forceinline__ void set_world(rtm::V3 o, rtm::V3 id) {
+    if (kColdWorld) {
+      cold(6) = pack(o.x, o.y);
+      cold(7) = pack(o.z, id.x);
+      cold(8) = pack(id.y, id.z);
+    } else {
+      O = o;
+      idir = id;
+    }
+  }
+  __device__ __forceinline__ rtm::V3 world_o() const {
+    if (!kColdWorld) return O;
+    const unsigned long long a = cold(6), b = cold(7);
+    return rtm::v3(lo(a), hi(a), lo(b));
+  }
+  __device__ __forceinline__ rtm::V3 world_idir() const {
+    if (!kColdWorld) return idir;
+    const unsigned long long b = cold(7), c = cold(8);
+    return rtm::v3(hi(b), lo(c), hi(c));
+  }
+  // one visit of the trace (the reference's MemoryTransactionRecord)
+  __device__ __forceinline__ void record(uint32_t unit, uint32_t type) {
+    if (rec.n < rec.cap) {
+      uint32_t* vrow = reinterpret_cast<uint32_t*>(cold(4));
+      uint32_t* trow = reinterpret_cast<uint32_t*>(cold(5));
+      if (vrow) vrow[rec.n] = rtf::pack_visit(unit, type);
+      if (trow) trow[rec.n] = v.meta[unit].x;
+    }
+    rec.n++;
+    rec.bytes += rtf::tx_bytes(type);
   }
 
   // Staged location (dense treelet << 10 | slot) of the node the ray visits
@@ -86,28 +152,31 @@ struct Walker {
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
     v = scene_of<MULTI>(a, r);
-    load_ray(a.rays, r, O, tmin, D, tmax);
+    rtm::V3 o, D;
+    load_ray(a.rays, r, o, tmin, D, tmax);
     const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
     terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
-    rec = Recorder{a.visits ? a.visits + (uint64_t)r * a.cap : nullptr,
-                   a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr, a.cap, 0u, 0u, v.meta};
+    cold(4) = reinterpret_cast<unsigned long long>(a.visits ? a.visits + (uint64_t)r * a.cap : nullptr);
+    cold(5) = reinterpret_cast<unsigned long long>(a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr);
+    rec = Counts{a.cap, 0u, 0u};
     status = 0;
     clear();
     min_thit = tmax;
-    c_leaf = c_inst = 0;
-    c_tobj = 0.0f;
+    set_hit(0, 0, 0.0f);
+    set_dir(D);
     ic.unit = kNone;
     smem_reads = gmem_reads = 0;
-    idir = rtm::calculate_idir(D);
-    fast = rtd::finite_ray(O, D, tmin, tmax);
+    const rtm::V3 id = rtm::calculate_idir(D);
+    set_world(o, id);
+    fast = rtd::finite_ray(o, D, tmin, tmax);
     ic_fast = false;
-    rec.rec(0, rtf::TX_STRUCTURE);
+    record(0, rtf::TX_STRUCTURE);
     const uint4 h0 = __ldg(v.blob), h1 = __ldg(v.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
     const rtm::V3 bmax = rtm::v3(__uint_as_float(h1.y), __uint_as_float(h1.z), __uint_as_float(h1.w));
     float th;
-    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) {
+    if (rtm::ray_box_test(bmin, bmax, id, o, tmin, tmax, th)) {
       // current_treelet_root starts as the TLAS header, unit 0 (:1707)
       const uint32_t code = ((uint32_t)(root_off >> 6) << kEShift) | kTop;
       const uint32_t unit = code >> kEShift;
@@ -184,11 +253,11 @@ struct Walker {
       enter = inst;
     }
     if (enter != kNone) {
-      enter_instance(in, enter, O, D, tmin, tmax, ic);
+      enter_instance(in, enter, world_o(), dir(), tmin, tmax, ic);
       ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
     }
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
-      rec.rec(unit, rtf::TX_INTERNAL);
+      record(unit, rtf::TX_INTERNAL);
       uint32_t soff01 = 0, soff23 = 0, soff45 = 0;
       if (pinned) {  // route bits in bytes 16..17, child records in the tail
         const uint4 t = rtd::ld_shared_v4(saddr + rtp::IN_UNIT);
@@ -201,7 +270,7 @@ struct Walker {
       }
       // one box test for both levels, so lanes at TLAS and BLAS nodes run it together
       const bool f = top ? fast : ic_fast;
-      const rtm::V3 o = top ? O : ic.o, id = top ? idir : ic.idir;
+      const rtm::V3 o = top ? world_o() : ic.o, id = top ? world_idir() : ic.idir;
       const float t0 = top ? tmin : ic.tmin, t1 = top ? tmax : ic.tmax;
       const float cull = top ? min_thit : min_thit * ic.mult;
       const rtd::ChildHits ch = f ? rtd::test_children<true>(nd, unit, o, id, t0, t1, cull)
@@ -224,7 +293,7 @@ struct Walker {
         c += ci & 3u;
       }
     } else if (top) {  // instance leaf (:1870-1953)
-      rec.rec(unit, rtf::TX_INSTANCE_LEAF);
+      record(unit, rtf::TX_INSTANCE_LEAF);
       uint32_t hdr_unit, broot_unit, broot_soff = 0;
       if (pinned) {  // the 64-byte record: units, route bits, BLAS root record, rows
         hdr_unit = nd.w[rtp::IL_HDR_UNIT / 4];
@@ -240,11 +309,11 @@ struct Walker {
         const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
         broot_unit = (uint32_t)(broot >> 6);
       }
-      rec.rec(hdr_unit, rtf::TX_STRUCTURE);
+      record(hdr_unit, rtf::TX_STRUCTURE);
       const uint32_t cc = broot_soff ? ((broot_soff << kEShift) | kEPin) : (broot_unit << kEShift);
       push((rbits >> (kRouteInst + rsh)) & 1u, cc, unit);
     } else {  // primitive leaf (:2071-2196)
-      rec.rec(unit, rtf::TX_LEAF_DESC);
+      record(unit, rtf::TX_LEAF_DESC);
       const rtd::Node64& q = nd;
       if (rtf::leaf_type_of(q.w[1]) == 0) {
         const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
@@ -255,17 +324,15 @@ struct Walker {
         const float wt = t / ic.mult;
         if (hit && tmin <= wt && wt <= tmax && wt < min_thit) {  // :2127-2141
           min_thit = t / ic.mult;
-          c_tobj = t;
-          c_leaf = unit;
-          c_inst = inst;
-          rec.rec(unit, rtf::TX_QUAD_LEAF_HIT);
+          set_hit(unit, inst, t);
+          record(unit, rtf::TX_QUAD_LEAF_HIT);
           if (terminate) clear();
         } else {
-          rec.rec(unit, rtf::TX_QUAD_LEAF);
+          record(unit, rtf::TX_QUAD_LEAF);
         }
       } else {
         status |= RT_RAY_HIT_PROCEDURAL;
-        rec.rec(unit, rtf::TX_PROCEDURAL_LEAF);
+        record(unit, rtf::TX_PROCEDURAL_LEAF);
       }
     }
     if (status & RT_RAY_STACK_OVERFLOW) clear();
@@ -277,19 +344,22 @@ struct Walker {
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
     const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);
-    write_hit(a, v, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
+    const unsigned long long h = cold(2);
+    const Recorder counts{nullptr, nullptr, rec.cap, rec.n, rec.bytes, v.meta};
+    write_hit(a, v, r, !bad && (min_thit < tmax), min_thit, world_o(), dir(), tmin, tmax, (uint32_t)h,
+              (uint32_t)(h >> 32), lo(cold(3)), counts, status);
   }
 };
 
 // The walker's stacks are a separate local array so that its fields stay in
-// registers, capped at 85 by three 256-thread CTAs per SM: +5% over the
-// walker with its stacks inside (whose fields the compiler left in local
-// memory), and better than caps of 51 or 64 (spills) or none (99 registers).
-constexpr int kTreeletMinBlocks = 3;
+// registers (+5% over the walker with its stacks inside, whose fields the
+// compiler left in local memory); with its rarely used fields in the stack's
+// cold tail it fits four 256-thread CTAs per SM at 64 registers.
+constexpr int kTreeletMinBlocks = 4;
 
 template <int CAP, bool MULTI>
 __global__ void __launch_bounds__(256, kTreeletMinBlocks) trace_treelet_kernel(TraceArgs a) {
-  unsigned long long stack[2 * CAP];
+  unsigned long long stack[2 * CAP + kColdWords];
   Walker<CAP, false, MULTI> w;
   w.stk = stack;
   w.pin_base = 0;
@@ -432,7 +502,7 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_sta
       if (st.resident[s] == d && u < st.units[s]) return slot_base + s * a.slot_bytes + u * 64u;
     return 0u;
   };
-  unsigned long long stack[2 * CAP];
+  unsigned long long stack[2 * CAP + kColdWords];
   Walker<CAP, true, false> w;  // staged launches trace one scene
   w.stk = stack;
   w.pin_base = pin_ok ? smem_u32(smem0) : 0u;
@@ -481,7 +551,8 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_sta
         uint32_t key = nl == kNone ? kNone : (nl >> kSlotBitsDev);
         if (a.hint && key != kNone) {
           // vote for the treelet predicted to follow the one the ray enters next
-          const uint32_t oct = (w.D.x > 0.0f ? 1u : 0u) | (w.D.y > 0.0f ? 2u : 0u) | (w.D.z > 0.0f ? 4u : 0u);
+          const rtm::V3 wd = w.dir();
+          const uint32_t oct = (wd.x > 0.0f ? 1u : 0u) | (wd.y > 0.0f ? 2u : 0u) | (wd.z > 0.0f ? 4u : 0u);
           key = __ldg(a.hint + (size_t)key * 8 + oct);
           if (key >= a.n_treelets) key = kNone;
         }
