@@ -56,8 +56,8 @@ def _peaks():
 # the ncu capture summarised in profiles/trace_kernels_terrain_instances.md: the same scene with
 # 262,144 rays per launch (the full launch of 2,097,152 rays is too large to capture with
 # --set full); scaled to a full launch by the ray count.
-STAGED_DRAM_BYTES_PER_RAY = {"primary": (104.267264e6 + 14.503936e6) / 262144,
-                             "bounce": (169.227520e6 + 30.532608e6) / 262144}
+STAGED_DRAM_BYTES_PER_RAY = {"primary": (103.862784e6 + 16.576000e6) / 262144,
+                             "bounce": (171.958528e6 + 33.870336e6) / 262144}
 
 
 def _traffic_per_ray():
