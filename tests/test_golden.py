@@ -260,3 +260,35 @@ def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases,
         if not np.array_equal(digest(np.array(words, np.uint64)), g[f"{name}__digests"][i]):
             bad.append(i)
     assert not bad, (name, "cases differing from the reference:", bad[:10])
+
+
+def test_reference_walk_timing_mode(built, tmp_path):
+    """The timing mode of the reference-walk harness (the CPU baseline of
+    bench.py) traces a batch on several threads and reports one line per
+    pass; its untimed results mode agrees with the oracle on the same rays.
+    Skipped where the harness is not built (no reference tree and no
+    extracted sources)."""
+    import subprocess
+
+    import treelet_rt as rt
+    from helpers import reference_words
+    from oracle import oracle as orc
+
+    harness = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                           "pin_traversal")
+    if not os.path.exists(harness):
+        pytest.skip("reference walk harness not built")
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 2048, 9).bytes()
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 40, 40, 1, 2, 1e-4, 1e30)
+    bp, rp, op = (str(tmp_path / x) for x in ("blob", "rays", "out"))
+    blob.tofile(bp)
+    rays.tofile(rp)
+    r = subprocess.run([harness, "--time", bp, rp, "0", "1", "8192", "4", "3"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    reps = [ln.split() for ln in r.stderr.splitlines() if ln.startswith("rep ")]
+    assert [int(x[1]) for x in reps] == [0, 1, 2] and all(float(x[2]) > 0 for x in reps)
+    subprocess.run([harness, bp, rp, "0", "1", "8192", "0", op], check=True, capture_output=True, timeout=300)
+    words = np.fromfile(op, np.uint32)
+    hits, vis, _ = orc.trace(blob, rays, 0, default_flags=1, capacity=1024, want_visits=True)
+    assert np.array_equal(np.concatenate(reference_words(hits, vis, None, 0)), words)
