@@ -251,11 +251,13 @@ rt_status rt_trace(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, u
  * pointers are then host pointers) out; synchronous.  When `hits` is
  * page-locked, mapped host memory (cudaHostAlloc, or cudaHostRegister with
  * mapping) and no trace is asked for, the kernel writes the hit records
- * straight into it and there is no copy-out.  Otherwise a call of 2^19 rays
- * or more runs as up to 4 chunks on the scene's own streams, so that copies
- * of one chunk overlap the trace of another (page-locked host arrays let them
- * overlap fully).  Results and the counters of rt_trace_stats_get cover the
- * whole call, as for one rt_trace. */
+ * straight into it and there is no copy-out; if `rays` (and `flags`) are
+ * page-locked too, the kernel also reads them where they are, and the call is
+ * one launch with no copies.  Otherwise a call of 2^19 rays or more runs as up
+ * to 4 chunks on the scene's own streams, so that copies of one chunk overlap
+ * the trace of another (page-locked host arrays let them overlap fully).
+ * Results and the counters of rt_trace_stats_get cover the whole call, as for
+ * one rt_trace. */
 rt_status rt_trace_host(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                         uint32_t n, uint32_t mode, rt_hit* hits, const rt_trace_buf* trace);
 

@@ -745,9 +745,18 @@ rt_status rt_trace_host(rt_scene* s, const rt_ray* rays, const uint32_t* flags, 
   // Page-locked hit records: the kernel writes them straight into host memory
   // as rays finish, so no copy-out follows the trace and one launch over all
   // rays needs no chunks (chunked launches each pay a tail of long rays).
-  // Rays and flags are copied in first, in one copy each.
+  // Page-locked rays (and flags) are read by the kernel where they are, each
+  // once, when a lane takes its ray; pageable ones are copied in first, in one
+  // copy each.
   if (!cap) {
     rt_hit* mapped_hits = static_cast<rt_hit*>(mapped_host(hits));
+    const rt_ray* mapped_rays = mapped_hits ? static_cast<const rt_ray*>(mapped_host(rays)) : nullptr;
+    const uint32_t* mapped_flags = (mapped_rays && flags) ? static_cast<const uint32_t*>(mapped_host(flags)) : nullptr;
+    if (mapped_rays && (!flags || mapped_flags)) {
+      st = trace_launch(s, mapped_rays, mapped_flags, default_flags, n, mode, mapped_hits, nullptr, s->stream,
+                        s->d_queue, false);
+      return host_finish(s, st);
+    }
     if (mapped_hits) {
       const size_t b_rays = al(sizeof(rt_ray) * (size_t)n), b_flags = flags ? sizeof(uint32_t) * (size_t)n : 0;
       if (b_rays + b_flags > s->io_bytes) {
