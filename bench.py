@@ -346,8 +346,9 @@ def run_gpu(args, rank: int, world: int) -> None:
         check(lib().rt_trace_host(scene.handle, hr.data_ptr(), None, rt.RAY_FLAG_OPAQUE, n_prim, rt.MODE_STAGED,
                                   h_hits.data_ptr(), None))
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, args.warmup)):  # both batches, so every host buffer is touched first
         host_trace(h_prim, "primary")
+        host_trace(h_bounce, "bounce")
     e2e_t = []
     for _ in range(max(3, args.steps // 2)):
         flush.fill_(1.0)
