@@ -1,10 +1,11 @@
 """ctypes wrapper of liboracle_rt.so: the CPU restatement of the reference's
-traversal, treelet partition and prefetch decision.
+traversal, treelet partition and RT-unit rules (prefetch decision, warp
+selection, stride prefetcher) and the RT-unit trace replay.
 
 TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
 baseline of bench.py use it, as the checker.  See oracle_rt.h for the parity
-status (decoders pinned against the reference's header; traversal, treelets
-and prefetch decision unpinned: no reference tests or golden vectors exist).
+status: everything but the replay's memory model is pinned against the
+reference's own code, compiled in place by oracle/ref_pin/ (tests/golden/).
 """
 from __future__ import annotations
 
@@ -69,6 +70,10 @@ def lib():
         L.oracle_decode_node.argtypes = [vp, C.c_uint32, C.c_int, vp]
         L.oracle_geometry.restype = C.c_int
         L.oracle_geometry.argtypes = [C.c_int, vp, C.c_uint32, vp]
+        L.oracle_schedule_warp.restype = C.c_int
+        L.oracle_schedule_warp.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp]
+        L.oracle_stride_events.restype = C.c_int64
+        L.oracle_stride_events.argtypes = [C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, vp, C.c_uint64]
         L.oracle_unit_replay.restype = C.c_int
         L.oracle_unit_replay.argtypes = [vp, C.c_int, C.c_uint64, vp, vp, C.c_uint32, C.c_uint32, vp, vp, C.c_int]
         _lib = L
@@ -181,6 +186,35 @@ def unit_replay(treelets: Treelets, hits: np.ndarray, visits: np.ndarray, config
     if rc != 0:
         raise OracleError(lib().oracle_last_error().decode())
     return out
+
+
+def schedule_warp(treelets: Treelets, scheduler: int, treelet_prefetch: bool, last_prefetched: int,
+                  ready: np.ndarray, next_unit: np.ndarray) -> int:
+    """The RT unit's warp selection over resident warps in uid order
+    (rt_unit::schedule_next_warp, shader.cc:4307-4392): ready[i] is the warp's
+    !is_stalled(), next_unit[i, lane] its lanes' next access units (0xFFFFFFFF
+    for none).  Returns the chosen position or -1."""
+    rd = np.ascontiguousarray(ready, np.uint8)
+    nu = np.ascontiguousarray(next_unit, np.uint32).reshape(len(rd), 32)
+    return int(lib().oracle_schedule_warp(treelets.h, scheduler, int(treelet_prefetch), last_prefetched, len(rd),
+                                          rd.ctypes.data, nu.ctypes.data))
+
+
+def stride_events(warp_id: np.ndarray, next_addr: np.ndarray, pops: np.ndarray, max_queue: int,
+                  prefill: int = 0) -> np.ndarray:
+    """Demand accesses through one Lee stride prefetcher and its queue
+    (shader.cc:4779-4828), the queue starting with `prefill` entries
+    (request = base = 32 (i + 1)).  Returns the uint64 words: per event removed,
+    appended, per appended entry (request, base), queue length."""
+    wid = np.ascontiguousarray(warp_id, np.uint32)
+    na = np.ascontiguousarray(next_addr, np.uint64)
+    po = np.ascontiguousarray(pops, np.uint32)
+    out = np.zeros(7 * len(wid) + 8, np.uint64)
+    n = lib().oracle_stride_events(len(wid), wid.ctypes.data, na.ctypes.data, po.ctypes.data, max_queue, prefill,
+                                   out.ctypes.data, len(out))
+    if n < 0:
+        raise OracleError("stride_events: output too small")
+    return out[:n]
 
 
 def prefetch_decide(treelets: Treelets, next_unit: np.ndarray, heuristic: int = 0, max_queue: int = 1000000,

@@ -1190,6 +1190,96 @@ struct LaneTrace {
   bool issued = false;
 };
 
+// rt_unit::schedule_next_warp (shader.cc:4307-4392) over n resident warps
+// in uid order (m_current_warps is a std::map keyed by uid): `ready(i)` is
+// !is_stalled(), `matches(i)` counts the warp's lanes whose next access lies
+// in the last prefetched treelet.  scheduler 1 (OMR): the first ready warp
+// with a match; 2 (PMR): the first ready warp with the most matches; either
+// falls back, and scheduler 0 or no treelet prefetcher uses, the first ready
+// warp.  Returns its position or -1.
+template <class Ready, class Matches>
+int pick_warp(uint32_t n, uint32_t scheduler, bool treelet_prefetch, Ready ready, Matches matches) {
+  if (treelet_prefetch && scheduler == 1) {
+    for (uint32_t i = 0; i < n; ++i)
+      if (ready(i) && matches(i) > 0) return (int)i;
+  } else if (treelet_prefetch && scheduler == 2) {
+    int best = -1, best_count = 0;
+    for (uint32_t i = 0; i < n; ++i)
+      if (ready(i)) {
+        const int c = matches(i);
+        if (c > best_count) {
+          best = (int)i;
+          best_count = c;
+        }
+      }
+    if (best >= 0) return best;
+  }
+  for (uint32_t i = 0; i < n; ++i)
+    if (ready(i)) return (int)i;
+  return -1;
+}
+
+// The Lee MICRO'10 stride prefetcher (shader.cc:4792-4828 as written: the last
+// address is only recorded on a warp's first access, and prefetches are
+// queued only while the queue holds at least max_prefetch_queue_size
+// entries).  step() trains on one demand access and returns true with the
+// first prefetch address when two 32-byte prefetches are queued.
+struct LeeStride {
+  std::map<uint32_t, std::map<int, int>> pws_table;  // warp -> stride -> count
+  std::map<uint32_t, uint64_t> pws_last;
+  bool step(uint32_t wid, uint64_t next_addr, uint64_t queue_size, uint64_t max_queue, uint64_t* prefetch_addr) {
+    if (pws_table.count(wid) == 0) {
+      pws_last[wid] = next_addr;
+    } else if (pws_table[wid].size() <= 32) {
+      const int stride = (int)(uint32_t)(next_addr - pws_last[wid]);
+      pws_table[wid][stride]++;
+    }
+    int largest_stride = 0, largest_count = 0;
+    for (auto& kv : pws_table[wid])
+      if (kv.second > largest_count) {
+        largest_stride = kv.first;
+        largest_count = kv.second;
+      }
+    *prefetch_addr = next_addr + (uint64_t)(int64_t)largest_stride;
+    return max_queue <= queue_size;
+  }
+};
+
+// prefetch_mem_access_q: (request, base) pairs, with a count of the live
+// copies of each request address.
+struct PrefetchQueue {
+  std::deque<std::pair<uint64_t, uint64_t>> q;
+  std::unordered_map<uint64_t, uint32_t> live;
+
+  // The removal of queued prefetches of a demand-loaded address
+  // (shader.cc:4657-4668, 4779-4789 as written): erasing entry idx and then
+  // stepping to idx + 1 skips the entry that moved into its place.  An
+  // address with no live copy erases nothing, so the loop is skipped for it.
+  uint32_t remove(uint64_t addr) {
+    auto c = live.find(addr);
+    if (c == live.end() || c->second == 0) return 0;
+    uint32_t removed = 0;
+    for (size_t idx = 0; idx < q.size(); idx++) {
+      if (addr == q[idx].first) {
+        q.erase(q.begin() + (long)idx);
+        c->second--;
+        removed++;
+      }
+    }
+    return removed;
+  }
+  void push(uint64_t addr, uint64_t base) {
+    q.emplace_back(addr, base);
+    live[addr]++;
+  }
+  std::pair<uint64_t, uint64_t> pop() {
+    const auto r = q.front();
+    q.pop_front();
+    live[r.first]--;
+    return r;
+  }
+};
+
 struct UnitWarp {
   uint32_t wid = 0;  // warp id of the stride tables
   LaneTrace lane[32];
@@ -1216,16 +1306,14 @@ struct UnitReplay {
   std::vector<CacheLine> lines;
   std::vector<PrefetchRecord> records;
   std::map<uint64_t, int64_t> last_evicted;  // sector -> most recently evicted prefetch record
-  std::deque<std::pair<uint64_t, uint64_t>> pq;  // prefetch_mem_access_q: (request, base)
-  std::unordered_map<uint64_t, uint32_t> queued;  // live copies of each address in pq
+  PrefetchQueue pq;  // prefetch_mem_access_q
   std::deque<Request> chunk_q;                 // mem_access_q of the warp being served
   UnitWarp* serving = nullptr;
   std::list<UnitWarp> resident;                // m_current_warps, oldest first
   std::deque<std::pair<uint64_t, uint64_t>> metadata_returns;  // (cycle, base)
   uint64_t most_recent_metadata = 0;
   rt_prefetch_state dstate{0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0};
-  std::map<uint32_t, std::map<int, int>> pws_table;  // Lee: warp -> stride -> count
-  std::map<uint32_t, uint64_t> pws_last;
+  LeeStride lee;  // Lee stride tables
 
   UnitReplay(const oracle_treelets* t, const rt_unit_config& c) : tl(t), cfg(c) {}
 
@@ -1322,25 +1410,10 @@ struct UnitReplay {
     return meta_base + (uint64_t)metadata_idx[root] * meta_size;  // operator[]: 0 for a non-root
   }
 
-  // Removes queued prefetches of this address, stepping past the entry that
-  // follows each erased one (shader.cc:4657-4668 as written).
-  // (An address with no queued copy erases nothing, so the loop is skipped
-  // for it: `queued` counts the live copies of each address.)
-  void remove_queued(uint64_t addr) {
-    auto q = queued.find(addr);
-    if (q == queued.end() || q->second == 0) return;
-    for (size_t idx = 0; idx < pq.size(); idx++) {
-      if (addr == pq[idx].first) {
-        pq.erase(pq.begin() + (long)idx);
-        q->second--;
-        st.prefetch_removed++;
-      }
-    }
-  }
+  void remove_queued(uint64_t addr) { st.prefetch_removed += pq.remove(addr); }
 
   void enqueue(uint64_t addr, uint64_t base) {
-    pq.emplace_back(addr, base);
-    queued[addr]++;
+    pq.push(addr, base);
     st.prefetch_queued++;
   }
 
@@ -1356,24 +1429,9 @@ struct UnitReplay {
     for (int i = 0; i < (m.size + 31) / 32; ++i) enqueue(a + 32ull * i, a);
   }
 
-  // Lee MICRO'10 (shader.cc:4792-4826 as written: the last address is only
-  // recorded on a warp's first access; prefetches are queued only while the
-  // queue holds at least max_prefetch_queue_size entries).
   void stride_prefetch(uint32_t wid, uint64_t next_addr) {
-    if (pws_table.count(wid) == 0) {
-      pws_last[wid] = next_addr;
-    } else if (pws_table[wid].size() <= 32) {
-      const int stride = (int)(uint32_t)(next_addr - pws_last[wid]);
-      pws_table[wid][stride]++;
-    }
-    int largest_stride = 0, largest_count = 0;
-    for (auto& kv : pws_table[wid])
-      if (kv.second > largest_count) {
-        largest_stride = kv.first;
-        largest_count = kv.second;
-      }
-    const uint64_t pa = next_addr + (uint64_t)(int64_t)largest_stride;
-    if (cfg.decision.max_queue <= pq.size())
+    uint64_t pa = 0;
+    if (lee.step(wid, next_addr, pq.q.size(), cfg.decision.max_queue, &pa))
       for (unsigned i = 0; i < 2; ++i) enqueue(pa + i * 32, pa);
   }
 
@@ -1381,7 +1439,7 @@ struct UnitReplay {
     std::vector<uint32_t> next;
     for (auto& w : resident)
       for (auto& l : w.lane) next.push_back(l.ptr < l.end ? (l.row[l.ptr] >> 3) : 0xFFFFFFFFu);
-    dstate.queue_len = (uint32_t)pq.size();
+    dstate.queue_len = (uint32_t)pq.q.size();
     rt_prefetch_decision d;
     oracle_prefetch_decide(tl, next.data(), (uint32_t)next.size(), &cfg.decision, &dstate, &d);
     st.decisions++;
@@ -1396,38 +1454,23 @@ struct UnitReplay {
     }
   }
 
-  // rt_unit::schedule_next_warp (shader.cc:4307-4392)
+  // rt_unit::schedule_next_warp (shader.cc:4307-4392): pick_warp over the
+  // resident warps, oldest (lowest uid) first.
   UnitWarp* schedule() {
-    auto ready = [](const UnitWarp& w) { return !w.in_flight && !w.done(); };
-    const bool treelet = cfg.prefetcher == RT_UNIT_PF_TREELET;
-    auto matches = [&](const UnitWarp& w) {
+    std::vector<UnitWarp*> ws;
+    for (auto& w : resident) ws.push_back(&w);
+    auto ready = [&](uint32_t i) { return !ws[i]->in_flight && !ws[i]->done(); };
+    auto matches = [&](uint32_t i) {
       int c = 0;
-      for (const auto& l : w.lane)
+      for (const auto& l : ws[i]->lane)
         if (l.ptr < l.end) {
           const uint8_t* r = root_of_addr((uint64_t)(l.row[l.ptr] >> 3) * 64);
           if (dstate.last_prefetched != 0xFFFFFFFFu && r == tl->base + (uint64_t)dstate.last_prefetched * 64) ++c;
         }
       return c;
     };
-    if (treelet && cfg.scheduler == RT_UNIT_SCHED_OMR) {
-      for (auto& w : resident)
-        if (ready(w) && matches(w) > 0) return &w;
-    } else if (treelet && cfg.scheduler == RT_UNIT_SCHED_PMR) {
-      UnitWarp* best = nullptr;
-      int best_count = 0;
-      for (auto& w : resident)
-        if (ready(w)) {
-          const int c = matches(w);
-          if (c > best_count) {
-            best = &w;
-            best_count = c;
-          }
-        }
-      if (best) return best;
-    }
-    for (auto& w : resident)
-      if (ready(w)) return &w;
-    return nullptr;
+    const int k = pick_warp((uint32_t)ws.size(), cfg.scheduler, cfg.prefetcher == RT_UNIT_PF_TREELET, ready, matches);
+    return k < 0 ? nullptr : ws[k];
   }
 
   void start_round(UnitWarp* w) {
@@ -1469,7 +1512,7 @@ struct UnitReplay {
   }
 
   bool prefetch_issuable() {
-    const uint64_t base = pq.front().second;
+    const uint64_t base = pq.q.front().second;
     if (!cfg.wait_metadata || is_metadata(base)) return true;
     return most_recent_metadata == metadata_addr(root_of_addr(base));  // shader.cc:4469-4476
   }
@@ -1528,10 +1571,8 @@ struct UnitReplay {
       } else if (UnitWarp* w = schedule()) {
         start_round(w);
         send_demand(t);
-      } else if (cfg.prefetcher != RT_UNIT_PF_NONE && !pq.empty() && prefetch_issuable()) {
-        const auto req = pq.front();
-        pq.pop_front();
-        queued[req.first]--;
+      } else if (cfg.prefetcher != RT_UNIT_PF_NONE && !pq.q.empty() && prefetch_issuable()) {
+        const auto req = pq.pop();
         prefetch(req.first, req.second, t);
       }
     }
@@ -1558,6 +1599,60 @@ struct UnitReplay {
 };
 
 }  // namespace
+
+// rt_unit::schedule_next_warp over n resident warps (uid order): ready[i]
+// = !is_stalled(), next_unit[32 i + lane] = the lane's next access (unit) or
+// 0xFFFFFFFF; last_prefetched = root unit or 0xFFFFFFFF.  Returns the chosen
+// position or -1.
+extern "C" int oracle_schedule_warp(const oracle_treelets* tl, uint32_t scheduler, uint32_t treelet_prefetch,
+                                    uint32_t last_prefetched, uint32_t n, const uint8_t* ready,
+                                    const uint32_t* next_unit) {
+  auto is_ready = [&](uint32_t i) { return ready[i] != 0; };
+  auto matches = [&](uint32_t i) {
+    int c = 0;
+    for (int l = 0; l < 32; ++l) {
+      const uint32_t u = next_unit[32 * i + l];
+      if (u == 0xFFFFFFFFu || last_prefetched == 0xFFFFFFFFu) continue;
+      if (tl->addrToTreeletID(tl->base + (uint64_t)u * 64) == tl->base + (uint64_t)last_prefetched * 64) ++c;
+    }
+    return c;
+  };
+  return pick_warp(n, scheduler, treelet_prefetch != 0, is_ready, matches);
+}
+
+// A stream of demand accesses through one Lee stride prefetcher and its
+// prefetch queue, as the replay drives them.  The queue starts with `prefill`
+// entries (request = base = 32 (i + 1)).  Per event k, pops[k] entries
+// leave the queue front (issued), the queued copies of next_addr[k] are
+// removed, and warp_id[k]'s stride tables train on next_addr[k] and may queue
+// two prefetches.  out (uint64), per event: removed, appended, then per
+// appended entry (request, base), then the queue length.  Returns the number
+// of words written, or -1 when out_cap is too small.
+extern "C" int64_t oracle_stride_events(uint32_t n, const uint32_t* warp_id, const uint64_t* next_addr,
+                                        const uint32_t* pops, uint32_t max_queue, uint32_t prefill,
+                                        uint64_t* out, uint64_t out_cap) {
+  LeeStride lee;
+  PrefetchQueue pq;
+  for (uint32_t i = 0; i < prefill; ++i) pq.push(32ull * (i + 1), 32ull * (i + 1));
+  uint64_t w = 0;
+  for (uint32_t k = 0; k < n; ++k) {
+    for (uint32_t p = 0; p < pops[k] && !pq.q.empty(); ++p) pq.pop();
+    const uint32_t removed = pq.remove(next_addr[k]);
+    uint64_t pa = 0;
+    const bool queue = lee.step(warp_id[k], next_addr[k], pq.q.size(), max_queue, &pa);
+    if (w + 8 > out_cap) return -1;
+    out[w++] = removed;
+    out[w++] = queue ? 2 : 0;
+    if (queue)
+      for (unsigned i = 0; i < 2; ++i) {
+        pq.push(pa + i * 32, pa);
+        out[w++] = pa + i * 32;
+        out[w++] = pa;
+      }
+    out[w++] = pq.q.size();
+  }
+  return (int64_t)w;
+}
 
 extern "C" int oracle_unit_replay(const oracle_treelets* tl, int max_treelet_bytes, uint64_t blob_bytes,
                                   const rt_hit* hits, const uint32_t* visits, uint32_t n, uint32_t capacity,

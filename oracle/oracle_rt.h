@@ -10,10 +10,13 @@
  * (the decoder header unmodified; the geometry, createTreelets /
  * buildNodeToRootMap / remapBVHToTreeletLayout, traceRay and
  * traceRayWithTreelets as extracted line ranges), and the oracle is pinned
- * against their outputs (tests/golden/), as is its RT-unit prefetch decision
- * (the decision block of shader.cc's rt_unit::cycle, extracted and compiled
- * in a stand-in RT unit).  The RT-unit replay's memory model is this
- * project's own: no reference code pins it.
+ * against their outputs (tests/golden/), as are the RT-unit replay's
+ * treelet-prefetch decision (the decision block of shader.cc's
+ * rt_unit::cycle), its warp selection (rt_unit::schedule_next_warp) and its
+ * Lee stride prefetcher with the demand-load queue removal (blocks of
+ * rt_unit::memory_cycle), each extracted and compiled in a stand-in RT unit.
+ * The replay's memory model (cache, latencies, cycle loop) is this project's
+ * own: no reference code pins it.
  */
 #ifndef ORACLE_RT_H
 #define ORACLE_RT_H
@@ -82,6 +85,25 @@ int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit,
 int oracle_unit_replay(const oracle_treelets* tl, int max_treelet_bytes, uint64_t blob_bytes, const rt_hit* hits,
                        const uint32_t* visits, uint32_t n, uint32_t capacity, const rt_unit_config* cfg,
                        rt_unit_stats* stats, int threads);
+
+/* The RT unit's warp selection (rt_unit::schedule_next_warp, shader.cc:4307-4392)
+ * over n resident warps in uid order, as the replay uses it: ready[i] is
+ * !is_stalled(), next_unit[32 i + lane] the lane's next access (unit index)
+ * or 0xFFFFFFFF, last_prefetched a root unit or 0xFFFFFFFF.  Returns the
+ * chosen position or -1. */
+int oracle_schedule_warp(const oracle_treelets* tl, uint32_t scheduler, uint32_t treelet_prefetch,
+                         uint32_t last_prefetched, uint32_t n, const uint8_t* ready, const uint32_t* next_unit);
+
+/* A stream of demand accesses through one Lee MICRO'10 stride prefetcher and
+ * its prefetch queue (shader.cc:4779-4828), as the replay drives them: the
+ * queue starts with `prefill` entries (request = base = 32 (i + 1)); per
+ * event k, pops[k] entries leave the queue front, the queued copies of
+ * next_addr[k] are removed and warp_id[k]'s stride tables train on it and may
+ * queue two prefetches.  out (uint64), per event: removed, appended, per
+ * appended entry (request, base), queue length.  Returns the words written,
+ * or -1 when out_cap is too small. */
+int64_t oracle_stride_events(uint32_t n, const uint32_t* warp_id, const uint64_t* next_addr, const uint32_t* pops,
+                             uint32_t max_queue, uint32_t prefill, uint64_t* out, uint64_t out_cap);
 
 #ifdef __cplusplus
 }

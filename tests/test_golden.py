@@ -262,6 +262,116 @@ def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases,
     assert not bad, (name, "cases differing from the reference:", bad[:10])
 
 
+RTUNIT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rtunit.npz")
+
+
+def _rtunit_golden():
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_rtunit_golden
+
+    return make_rtunit_golden
+
+
+@pytest.mark.parametrize("name,budget,n_cases,seed", _rtunit_golden().SCHED_SCENES)
+def test_warp_selection_matches_reference_scheduler(built, name, budget, n_cases, seed):
+    """The replay's warp selection against the reference's own
+    rt_unit::schedule_next_warp (shader.cc:4307-4392, compiled in place by
+    oracle/ref_pin; fixtures made by tests/golden/make_rtunit_golden.py): for
+    every case under the oldest-first, OMR and PMR rules the chosen warp's
+    uid and the number of warps left resident."""
+    import hashlib
+
+    from oracle import oracle as orc
+
+    mk = _rtunit_golden()
+    from make_prefetch_golden import scene
+
+    g = np.load(RTUNIT)
+    blob = scene(name)
+    assert hashlib.sha256(blob.tobytes()).digest() == g[f"sched_{name}__scene_sha256"].tobytes(), "scene changed"
+    cases = mk.schedule_cases(blob, budget, n_cases, seed)
+    assert hashlib.sha256(mk.case_words(cases).tobytes()).digest() == g[f"sched_{name}__cases_sha256"].tobytes()
+    tl = orc.Treelets(blob, budget)
+    chosen, left = g[f"sched_{name}__chosen"], g[f"sched_{name}__left"]
+    assert len(chosen) == len(cases)
+    bad = []
+    for i, c in enumerate(cases):
+        k = orc.schedule_warp(tl, c["scheduler"], bool(c["treelet_prefetch"]), c["last_prefetched"],
+                              1 - c["stalled"], c["next_unit"])
+        uid = 0xFFFFFFFFFFFFFFFF if k < 0 else int(c["uids"][k])
+        if uid != int(chosen[i]) or len(c["uids"]) - (k >= 0) != int(left[i]):
+            bad.append(i)
+    assert not bad, (name, "cases differing from the reference:", bad[:10])
+    # every rule picked a warp somewhere, and OMR / PMR did not always agree with oldest-first
+    for rule in (1, 2):
+        picks = [(orc.schedule_warp(tl, rule, True, c["last_prefetched"], 1 - c["stalled"], c["next_unit"]),
+                  orc.schedule_warp(tl, 0, True, c["last_prefetched"], 1 - c["stalled"], c["next_unit"]))
+                 for c in cases]
+        assert any(a >= 0 for a, _ in picks) and any(a != b for a, b in picks), rule
+
+
+@pytest.mark.parametrize("i", range(len(_rtunit_golden().STRIDE_STREAMS)))
+def test_stride_prefetcher_matches_reference_block(built, i):
+    """The replay's Lee stride prefetcher and prefetch queue against the
+    reference's own blocks of rt_unit::memory_cycle (shader.cc:4779-4828: the
+    removal of queued copies of the demand address, the per-warp stride
+    training and the two queued prefetches), over seeded demand streams:
+    every event's removed and appended entries and the queue length."""
+    import hashlib
+
+    from oracle import oracle as orc
+
+    mk = _rtunit_golden()
+    max_queue, prefill, n_events, n_warps, seed = mk.STRIDE_STREAMS[i]
+    g = np.load(RTUNIT)
+    wid, addr, pops = mk.stride_streams(n_events, n_warps, seed)
+    ew = mk.stride_words(wid, addr, pops)
+    assert hashlib.sha256(ew.tobytes()).digest() == g[f"stride_{i}__events_sha256"].tobytes()
+    words = orc.stride_events(wid, addr, pops, max_queue, prefill)
+    assert len(words) == int(g[f"stride_{i}__n_words"][0])
+    assert np.array_equal(mk.digest(words), g[f"stride_{i}__digest"])
+
+
+def test_stride_prefetcher_as_written():
+    """Known answers of the reference's stride prefetcher as written
+    (shader.cc:4792-4828): a warp's strides are taken from its FIRST address,
+    the most frequent one wins with ties to the smallest, a stride is the
+    address difference cut to 32 bits, and two 32-byte prefetches are queued
+    only while the queue holds at least the limit; a demand address erases
+    its queued copies but skips the copy that moves into an erased slot."""
+    from oracle import oracle as orc
+
+    def run(addrs, max_queue=0, prefill=0, pops=None, warps=None):
+        n = len(addrs)
+        return orc.stride_events(np.zeros(n, np.uint32) if warps is None else np.array(warps, np.uint32),
+                                 np.array(addrs, np.uint64), np.zeros(n, np.uint32) if pops is None else
+                                 np.array(pops, np.uint32), max_queue, prefill).tolist()
+
+    a = 1 << 30
+    # first access: no stride yet, prefetch at the address itself (stride 0)
+    assert run([a]) == [0, 2, a, a, a + 32, a, 2]
+    # second access 64 later: stride 64 from the first address -> a + 128
+    w = run([a, a + 64])
+    assert w[7:] == [0, 2, a + 128, a + 128, a + 160, a + 128, 4]
+    # third access at a + 128 erases its queued copy; strides 64 and 128 tie -> 64
+    w = run([a, a + 64, a + 128])
+    assert w[14:] == [1, 2, a + 192, a + 192, a + 224, a + 192, 5]
+    # the difference is cut to 32 bits: 2^32 + 64 later trains stride 64
+    w = run([a, a + (1 << 32) + 64])
+    assert w[7:9] == [0, 2] and w[9] == a + (1 << 32) + 128
+    # the limit: an empty queue under a limit of 1 never fills; a queue of 2 under 2 queues
+    assert run([a, a + 64], max_queue=1) == [0, 0, 0, 0, 0, 0]
+    assert run([a], max_queue=2, prefill=2)[:2] == [0, 2]
+    # the skip: warp 1 queues (x - 32, x), then warp 0 (stride 4096) queues (x, x + 32) right behind it,
+    # x = a + 20480; a demand of x erases the first copy and steps past the second
+    x = a + 20480
+    w = run([a, a + 4096, x - 32, a + 16384, x], warps=[0, 0, 1, 0, 2])
+    assert w[21:28] == [0, 2, x, x, x + 32, x, 8]
+    assert w[28:] == [1, 2, x, x, x + 32, x, 9]
+
+
 def test_reference_walk_timing_mode(built, tmp_path):
     """The timing mode of the reference-walk harness (the CPU baseline of
     bench.py) traces a batch on several threads and reports one line per
