@@ -74,6 +74,7 @@ def lib():
         L.oracle_schedule_warp.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp]
         L.oracle_stride_events.restype = C.c_int64
         L.oracle_stride_events.argtypes = [C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, vp, C.c_uint64]
+        L.oracle_prefetch_tally.argtypes = [C.c_uint32, vp, vp, vp]
         L.oracle_unit_replay.restype = C.c_int
         L.oracle_unit_replay.argtypes = [vp, C.c_int, C.c_uint64, vp, vp, C.c_uint32, C.c_uint32, vp, vp, C.c_int]
         _lib = L
@@ -215,6 +216,17 @@ def stride_events(warp_id: np.ndarray, next_addr: np.ndarray, pops: np.ndarray, 
     if n < 0:
         raise OracleError("stride_events: output too small")
     return out[:n]
+
+
+def prefetch_tally(block: np.ndarray, effectiveness: np.ndarray) -> np.ndarray:
+    """The end-of-run tally of one RT unit's prefetch records (gpu-sim.cc:
+    1749-1795): the count per class (TOO_LATE, LATE, TIMELY, TOO_EARLY,
+    NEVER_USED), then the unclassified-but-accessed count."""
+    b = np.ascontiguousarray(block, np.uint64)
+    e = np.ascontiguousarray(effectiveness, np.uint8)
+    out = np.zeros(6, np.uint64)
+    lib().oracle_prefetch_tally(len(b), b.ctypes.data, e.ctypes.data, out.ctypes.data)
+    return out
 
 
 def prefetch_decide(treelets: Treelets, next_unit: np.ndarray, heuristic: int = 0, max_queue: int = 1000000,

@@ -1165,6 +1165,34 @@ struct PrefetchRecord {  // prefetch_block_info (gpu-cache.h:99-113), the fields
   int effectiveness = E_UNCLASSIFIED;
 };
 
+// The end-of-run tally of one RT unit's prefetch records (gpu-sim.cc:
+// 1749-1795): records are grouped by block address; in a block where some
+// record was classified (anything but UNCLASSIFIED and NEVER_USED), the
+// unclassified ones count as "unclassified but accessed" and the rest by
+// class; in a block where none was, the unclassified ones become NEVER_USED
+// and all count by class.
+template <class Rec, class Count>
+void tally_records(std::vector<Rec>& records, Count* effectiveness, Count& unclassified_but_accessed) {
+  std::map<uint64_t, std::vector<Rec*>> by_block;
+  for (auto& r : records) by_block[r.block].push_back(&r);
+  for (auto& kv : by_block) {
+    bool accessed = false;
+    for (auto* r : kv.second)
+      if (r->effectiveness != E_UNCLASSIFIED && r->effectiveness != E_NEVER_USED) accessed = true;
+    for (auto* r : kv.second) {
+      if (accessed) {
+        if (r->effectiveness == E_UNCLASSIFIED) {
+          unclassified_but_accessed++;
+          continue;
+        }
+      } else if (r->effectiveness == E_UNCLASSIFIED) {
+        r->effectiveness = E_NEVER_USED;
+      }
+      effectiveness[r->effectiveness]++;
+    }
+  }
+}
+
 struct SectorState {
   bool valid = false;
   uint64_t ready = 0;  // cycle the data is there
@@ -1576,25 +1604,7 @@ struct UnitReplay {
         prefetch(req.first, req.second, t);
       }
     }
-    // final tally (gpu-sim.cc:1749-1790)
-    std::map<uint64_t, std::vector<PrefetchRecord*>> by_block;
-    for (auto& r : records) by_block[r.block].push_back(&r);
-    for (auto& kv : by_block) {
-      bool accessed = false;
-      for (auto* r : kv.second)
-        if (r->effectiveness != E_UNCLASSIFIED && r->effectiveness != E_NEVER_USED) accessed = true;
-      for (auto* r : kv.second) {
-        if (accessed) {
-          if (r->effectiveness == E_UNCLASSIFIED) {
-            st.unclassified_but_accessed++;
-            continue;
-          }
-        } else if (r->effectiveness == E_UNCLASSIFIED) {
-          r->effectiveness = E_NEVER_USED;
-        }
-        st.effectiveness[r->effectiveness]++;
-      }
-    }
+    tally_records(records, st.effectiveness, st.unclassified_but_accessed);
   }
 };
 
@@ -1652,6 +1662,17 @@ extern "C" int64_t oracle_stride_events(uint32_t n, const uint32_t* warp_id, con
     out[w++] = pq.q.size();
   }
   return (int64_t)w;
+}
+
+// The end-of-run tally over one RT unit's n prefetch records (block address,
+// class 0-5 as prefetch_request_effectiveness numbers them): out[0..4] the
+// count per class, out[5] the unclassified-but-accessed count.
+extern "C" void oracle_prefetch_tally(uint32_t n, const uint64_t* block, const uint8_t* effectiveness,
+                                      uint64_t* out) {
+  std::vector<PrefetchRecord> records(n);
+  for (uint32_t i = 0; i < n; ++i) records[i] = PrefetchRecord{block[i], (int)effectiveness[i]};
+  for (int k = 0; k < 6; ++k) out[k] = 0;
+  tally_records(records, out, out[5]);
 }
 
 extern "C" int oracle_unit_replay(const oracle_treelets* tl, int max_treelet_bytes, uint64_t blob_bytes,

@@ -14,7 +14,8 @@
  * treelet-prefetch decision (the decision block of shader.cc's
  * rt_unit::cycle), its warp selection (rt_unit::schedule_next_warp) and its
  * Lee stride prefetcher with the demand-load queue removal (blocks of
- * rt_unit::memory_cycle), each extracted and compiled in a stand-in RT unit.
+ * rt_unit::memory_cycle) and its end-of-run prefetch tally (gpu-sim.cc), each
+ * extracted and compiled in a stand-in RT unit.
  * The replay's memory model (cache, latencies, cycle loop) is this project's
  * own: no reference code pins it.
  */
@@ -104,6 +105,12 @@ int oracle_schedule_warp(const oracle_treelets* tl, uint32_t scheduler, uint32_t
  * or -1 when out_cap is too small. */
 int64_t oracle_stride_events(uint32_t n, const uint32_t* warp_id, const uint64_t* next_addr, const uint32_t* pops,
                              uint32_t max_queue, uint32_t prefill, uint64_t* out, uint64_t out_cap);
+
+/* The end-of-run tally of one RT unit's prefetch records (gpu-sim.cc:1749-1795)
+ * as the replay makes it: n records (block address, class 0-5 numbered as
+ * prefetch_request_effectiveness); out[0..4] the count per class, out[5] the
+ * unclassified-but-accessed count. */
+void oracle_prefetch_tally(uint32_t n, const uint64_t* block, const uint8_t* effectiveness, uint64_t* out);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,6 @@
-// Runs two more pieces of the REFERENCE's RT unit on batches of cases and
-// writes what they did: the golden data the replay's warp selection and
-// stride prefetcher are pinned against.
+// Runs three more pieces of the REFERENCE's RT-unit model on batches of cases
+// and writes what they did: the golden data the replay's warp selection,
+// stride prefetcher and prefetch tally are pinned against.
 //
 //  - rt_unit::schedule_next_warp (src/gpgpu-sim/shader.cc:4307-4392): which
 //    resident warp the RT unit serves next, under the OMR (1), PMR (2) or
@@ -9,12 +9,17 @@
 //  - the Lee MICRO'10 stride prefetcher of rt_unit::memory_cycle
 //    (shader.cc:4779-4828): the removal of queued prefetches of a demand
 //    address, then the per-warp stride training and the two queued prefetches.
+//  - the end-of-run tally of each RT unit's prefetch records into the
+//    effectiveness classes (src/gpgpu-sim/gpu-sim.cc:1749-1795), with the
+//    record struct prefetch_block_info (gpu-cache.h:99-131) and its class enum
+//    (abstract_hardware_model.h:247-254).
 //
 // The reference code is not copied here.  The Makefile in this folder extracts
-// both ranges, unmodified, into oracle/_ref/extract/ (rt_schedule.inc: the
-// definition of rt_unit::schedule_next_warp; rt_lee.inc: the two blocks) and
-// this file compiles them against its own stand-in class `rt_unit`, whose
-// members carry the names the code uses.
+// the ranges, unmodified, into oracle/_ref/extract/ (rt_schedule.inc: the
+// definition of rt_unit::schedule_next_warp; rt_lee.inc: the two blocks;
+// rt_effect.inc, rt_blockinfo.inc, rt_tally.inc) and this file compiles them
+// against its own stand-in classes `rt_unit` and TallyGpu, whose members
+// carry the names the code uses.
 //
 // Usage:
 //   pin_rtunit schedule <blob file> <max bytes per treelet> <cases file> <out file>
@@ -30,9 +35,18 @@
 //     `pops` entries leave the queue front first (issued prefetches).
 //     out (uint64 words), per event: removed, appended, per appended entry
 //     (request, base), queue length.
+//   pin_rtunit tally <records file> <out file>
+//     records (uint32 words): n_clusters, then per cluster: n_records, then
+//     per record: block address low, high, class (0-5).
+//     out (uint64 words): unclassified_but_accessed, the five class totals,
+//     then the per-cluster counts, class-major (cluster i, class c at
+//     i + c n_clusters).
 #include "treelet_env.h"
 
 #define RT_SCHEDULER_DPRINTF(...)
+
+#include "rt_effect.inc"
+#include "rt_blockinfo.inc"
 
 // ---- the warp instruction, as far as the scheduler and the prefetcher see it
 struct RTMemoryTransactionRecordStandIn {
@@ -69,6 +83,7 @@ class rt_unit {
   std::map<unsigned, new_addr_type> pws_last_accessed_addr;
   unsigned prefetches_removed_from_queue = 0;
   unsigned prefetches_added_to_queue = 0;
+  std::map<new_addr_type, std::vector<prefetch_block_info>> prefetch_request_tracker;
 
   void schedule_next_warp(warp_inst_t& inst);
 
@@ -78,6 +93,35 @@ class rt_unit {
 };
 
 #include "rt_schedule.inc"
+
+// ---- the GPU, as far as the end-of-run tally sees it
+struct TallyCore {
+  rt_unit unit;
+  rt_unit* get_m_rt_unit() { return &unit; }
+};
+struct TallyCluster {
+  TallyCore core;
+  TallyCore* cores[1] = {&core};
+  TallyCore** get_m_core() { return cores; }
+};
+struct TallyConfig {
+  unsigned n_clusters = 0;
+  unsigned num_cluster() const { return n_clusters; }
+};
+class TallyGpu {
+ public:
+  TallyConfig m_config;
+  std::vector<TallyCluster*> m_cluster;
+  unsigned out_unclassified_but_accessed = 0;
+  std::vector<unsigned> out_total, out_per_cluster;
+
+  void tally() {
+#include "rt_tally.inc"
+    out_unclassified_but_accessed = unclassified_but_accessed;
+    out_total = total_prefetch_effectiveness;
+    out_per_cluster = prefetch_effectiveness_per_cluster;
+  }
+};
 
 namespace {
 
@@ -165,13 +209,49 @@ int run_stride(int argc, char** argv) {
   return 0;
 }
 
+int run_tally(int argc, char** argv) {
+  if (argc != 4) return 2;
+  const std::vector<uint8_t> raw = read_file(argv[2]);
+  if (raw.size() % 4 || raw.empty()) return 2;
+  std::vector<uint32_t> w(raw.size() / 4);
+  memcpy(w.data(), raw.data(), raw.size());
+  TallyGpu gpu;
+  gpu.m_config.n_clusters = w[0];
+  std::vector<TallyCluster> clusters(w[0]);
+  size_t i = 1;
+  for (auto& c : clusters) {
+    gpu.m_cluster.push_back(&c);
+    if (i >= w.size()) return 2;
+    const uint32_t n = w[i++];
+    if (i + (size_t)n * 3 > w.size()) return 2;
+    for (uint32_t k = 0; k < n; ++k, i += 3) {
+      prefetch_block_info info;
+      info.m_block_addr = (new_addr_type)w[i] | ((new_addr_type)w[i + 1] << 32);
+      info.effectiveness = (prefetch_request_effectiveness)w[i + 2];
+      c.core.unit.prefetch_request_tracker[info.m_block_addr].push_back(info);
+    }
+  }
+  gpu.tally();
+  std::vector<uint64_t> out;
+  out.push_back(gpu.out_unclassified_but_accessed);
+  for (unsigned v : gpu.out_total) out.push_back(v);
+  for (unsigned v : gpu.out_per_cluster) out.push_back(v);
+  FILE* f = fopen(argv[3], "wb");
+  if (!f) return 2;
+  fwrite(out.data(), sizeof(uint64_t), out.size(), f);
+  fclose(f);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc >= 2 && strcmp(argv[1], "schedule") == 0) return run_schedule(argc, argv);
   if (argc >= 2 && strcmp(argv[1], "stride") == 0) return run_stride(argc, argv);
+  if (argc >= 2 && strcmp(argv[1], "tally") == 0) return run_tally(argc, argv);
   fprintf(stderr,
           "usage: pin_rtunit schedule <blob> <max bytes per treelet> <cases> <out>\n"
-          "       pin_rtunit stride <events> <max_queue> <prefill> <out>\n");
+          "       pin_rtunit stride <events> <max_queue> <prefill> <out>\n"
+          "       pin_rtunit tally <records> <out>\n");
   return 2;
 }

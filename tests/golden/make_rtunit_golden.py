@@ -1,5 +1,5 @@
-"""Generates tests/golden/rtunit.npz: seeded cases for two more pieces of the
-RT unit and what the REFERENCE's own code (run by the harness
+"""Generates tests/golden/rtunit.npz: seeded cases for three more pieces of
+the RT-unit model and what the REFERENCE's own code (run by the harness
 oracle/ref_pin/pin_rtunit.cpp) does with them.
 
 - Warp selection, rt_unit::schedule_next_warp (src/gpgpu-sim/shader.cc:
@@ -15,6 +15,11 @@ oracle/ref_pin/pin_rtunit.cpp) does with them.
   prefetches leaving the queue front in between, from an empty or a filled
   queue.  The fixture keeps an 8-byte BLAKE2b digest and the length of each
   stream's result words.
+- The end-of-run tally of the prefetch records (gpu-sim.cc:1749-1795): 1 to 4
+  RT units' records over a few hundred block addresses, each record in one of
+  the six classes, blocks all unclassified, all never used or mixed.  The
+  fixture keeps the tally words (unclassified-but-accessed, the class totals,
+  the per-unit counts).
 
 SHA-256 digests of the case words are kept as well; the test regenerates the
 cases with case_words() / stride_streams().
@@ -45,6 +50,36 @@ SCHED_SCENES = [("kat", 256, 300, 11), ("cube", 1024, 600, 12), ("shared", 512, 
 # limit start from a filled queue (and one shows that an empty one stays so).
 STRIDE_STREAMS = [(0, 0, 600, 1, 21), (0, 0, 900, 4, 22), (1, 0, 300, 2, 23), (4, 8, 1200, 6, 24),
                   (16, 16, 1200, 3, 25), (2, 40, 1500, 8, 27), (1000, 1200, 400, 2, 26)]
+
+
+# (units, records per unit, blocks, seed)
+TALLY_SETS = [(1, 0, 1, 31), (1, 50, 10, 32), (2, 800, 200, 33), (4, 1500, 300, 34), (3, 3000, 2500, 35)]
+
+
+def tally_records(n_units, n_records, n_blocks, seed):
+    """Seeded prefetch records: per unit (block addresses, classes 0-5)."""
+    rng = np.random.default_rng(seed)
+    blocks = (np.sort(rng.choice(1 << 30, size=n_blocks, replace=False)).astype(np.uint64) * np.uint64(32)
+              + np.uint64(1 << 40))
+    out = []
+    for _ in range(n_units):
+        # per block a bias: mostly unclassified, mostly never used, or mixed
+        bias = rng.integers(0, 3, size=n_blocks)
+        b = rng.integers(0, n_blocks, size=n_records)
+        p = np.array([[0.02, 0.02, 0.02, 0.02, 0.02, 0.9], [0.0, 0.0, 0.0, 0.0, 0.8, 0.2],
+                      [0.15, 0.15, 0.2, 0.15, 0.1, 0.25]])
+        cls = np.array([rng.choice(6, p=p[bias[k]]) for k in b], np.uint8)
+        out.append((blocks[b], cls))
+    return out
+
+
+def tally_words(units) -> np.ndarray:
+    out = [len(units)]
+    for blocks, cls in units:
+        out.append(len(blocks))
+        for a, c in zip(blocks.tolist(), cls.tolist()):
+            out += [a & 0xFFFFFFFF, a >> 32, c]
+    return np.array(out, np.uint32)
 
 
 def schedule_cases(blob, budget, n_cases, seed):
@@ -175,6 +210,15 @@ def main():
                 j += 2 + 2 * int(res[j + 1]) + 1
             print(f"stride {i}: max_queue {max_queue}, prefill {prefill}, {n_events} events, {appended} queued, "
                   f"{removed} removed")
+        for i, (n_units, n_records, n_blocks, seed) in enumerate(TALLY_SETS):
+            tw = tally_words(tally_records(n_units, n_records, n_blocks, seed))
+            tw.tofile(cp)
+            subprocess.run([PIN, "tally", cp, op], check=True, capture_output=True)
+            res = np.fromfile(op, np.uint64)
+            assert len(res) == 6 + 5 * n_units
+            arrays[f"tally_{i}__records_sha256"] = sha(tw)
+            arrays[f"tally_{i}__words"] = res
+            print(f"tally {i}: {n_units} units, unclassified but accessed {res[0]}, totals {res[1:6].tolist()}")
     np.savez_compressed(os.path.join(HERE, "rtunit.npz"), **arrays)
 
 

@@ -334,6 +334,27 @@ def test_stride_prefetcher_matches_reference_block(built, i):
     assert np.array_equal(mk.digest(words), g[f"stride_{i}__digest"])
 
 
+@pytest.mark.parametrize("i", range(len(_rtunit_golden().TALLY_SETS)))
+def test_prefetch_tally_matches_reference_block(built, i):
+    """The replay's end-of-run tally of the prefetch records against the
+    reference's own block (gpu-sim.cc:1749-1795, with prefetch_block_info and
+    its class enum, compiled in place by oracle/ref_pin): the
+    unclassified-but-accessed count, the five class totals and every RT unit's
+    counts, for 1 to 4 units' seeded records."""
+    import hashlib
+
+    from oracle import oracle as orc
+
+    mk = _rtunit_golden()
+    n_units, n_records, n_blocks, seed = mk.TALLY_SETS[i]
+    g = np.load(RTUNIT)
+    units = mk.tally_records(n_units, n_records, n_blocks, seed)
+    assert hashlib.sha256(mk.tally_words(units).tobytes()).digest() == g[f"tally_{i}__records_sha256"].tobytes()
+    per_unit = np.stack([orc.prefetch_tally(b, c) for b, c in units])  # (units, 6)
+    got = np.concatenate([[per_unit[:, 5].sum()], per_unit[:, :5].sum(axis=0), per_unit[:, :5].T.reshape(-1)])
+    assert np.array_equal(got.astype(np.uint64), g[f"tally_{i}__words"])
+
+
 def test_stride_prefetcher_as_written():
     """Known answers of the reference's stride prefetcher as written
     (shader.cc:4792-4828): a warp's strides are taken from its FIRST address,
