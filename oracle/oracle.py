@@ -66,6 +66,9 @@ def lib():
                                    C.c_uint32, C.c_int]
         L.oracle_prefetch_decide.restype = C.c_int
         L.oracle_prefetch_decide.argtypes = [vp, vp, C.c_uint32, C.POINTER(_Params), vp, vp]
+        L.oracle_prefetch_decide_ex.restype = C.c_int
+        L.oracle_prefetch_decide_ex.argtypes = [vp, vp, C.c_uint32, C.POINTER(_Params), vp, vp, C.c_uint32,
+                                                C.c_uint32]
         L.oracle_decode_node.restype = C.c_int
         L.oracle_decode_node.argtypes = [vp, C.c_uint32, C.c_int, vp]
         L.oracle_geometry.restype = C.c_int
@@ -230,13 +233,17 @@ def prefetch_tally(block: np.ndarray, effectiveness: np.ndarray) -> np.ndarray:
 
 
 def prefetch_decide(treelets: Treelets, next_unit: np.ndarray, heuristic: int = 0, max_queue: int = 1000000,
-                    threshold: float = 0.5, second_prefetch: bool = False, state: np.ndarray | None = None):
-    """One RT unit's decision.  Returns (decision, new state) as structured scalars."""
+                    threshold: float = 0.5, second_prefetch: bool = False, state: np.ndarray | None = None,
+                    queue_variant: bool = False, flush: bool = False):
+    """One RT unit's decision.  Returns (decision, new state) as structured
+    scalars.  queue_variant: the pipelined treelet queue's copy of the
+    decision (shader.cc:3780-3932); flush: -flush_prefetch_queue_on_new_treelet."""
     nu = np.ascontiguousarray(next_unit, np.uint32)
     st = np.zeros(1, STATE_DTYPE) if state is None else np.array(state, STATE_DTYPE).reshape(1).copy()
     if state is None:
         st["last_prefetched"] = st["last_prefetched_second"] = st["last_rejected"] = 0xFFFFFFFF
     out = np.zeros(1, DECISION_DTYPE)
     p = _Params(heuristic, max_queue, threshold, int(second_prefetch), 0)
-    lib().oracle_prefetch_decide(treelets.h, nu.ctypes.data, len(nu), C.byref(p), st.ctypes.data, out.ctypes.data)
+    lib().oracle_prefetch_decide_ex(treelets.h, nu.ctypes.data, len(nu), C.byref(p), st.ctypes.data,
+                                    out.ctypes.data, int(queue_variant), int(flush))
     return out[0], st[0]

@@ -1047,9 +1047,16 @@ int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* t
   return 0;
 }
 
-// shader.cc:3419-3683, one RT unit, one decision.
-int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
-                           const rt_prefetch_params* p, rt_prefetch_state* st, rt_prefetch_decision* out) {
+// One RT unit, one decision.  queue_variant 0: the decision block of
+// rt_unit::cycle (shader.cc:3419-3683).  1: the copy that the pipelined
+// treelet queue runs (shader.cc:3780-3932), which has no second-prefetch rule,
+// suppresses only a repeat of the last prefetched treelet, and sizes
+// heuristic 3 at half the treelet instead of its popularity.  flush: the
+// queue is cleared before a new treelet's chunks are queued
+// (-flush_prefetch_queue_on_new_treelet, :3579-3583 and :3894-3898).
+int oracle_prefetch_decide_ex(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
+                              const rt_prefetch_params* p, rt_prefetch_state* st, rt_prefetch_decision* out,
+                              uint32_t queue_variant, uint32_t flush) {
   const uint8_t* NONE = nullptr;
   auto to_ptr = [&](uint32_t u) -> const uint8_t* { return u == 0xFFFFFFFFu ? nullptr : tl->base + (uint64_t)u * 64; };
   auto to_unit = [&](const uint8_t* a) -> uint32_t { return a ? unit_of(tl->base, a) : 0xFFFFFFFFu; };
@@ -1095,7 +1102,8 @@ int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit,
     } else {
       const auto* m = members_of(prefetched_treelet_root);
       const int n = m ? (int)m->size() : 0;
-      num_nodes_to_prefetch = (int)(((double)n * percentage) + 0.5);
+      const double share = (queue_variant && p->heuristic == 3) ? 0.5 : percentage;
+      num_nodes_to_prefetch = (int)(((double)n * share) + 0.5);
       submit = true;
     }
   }
@@ -1105,9 +1113,10 @@ int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit,
   if (submit && prefetched_treelet_root != NONE) {  // :3562-3640
     const auto* nodes = members_of(prefetched_treelet_root);
     const int n_nodes = nodes ? (int)nodes->size() : 0;
-    if (last_prefetched != prefetched_treelet_root && last_second != prefetched_treelet_root) {
+    if (last_prefetched != prefetched_treelet_root && (queue_variant || last_second != prefetched_treelet_root)) {
       const int num = (p->heuristic == 2 || p->heuristic == 3) ? num_nodes_to_prefetch : n_nodes;
       if ((uint64_t)num + queue <= p->max_queue) {
+        if (flush) queue = 0;
         const int j0 = (p->heuristic == 3) ? n_nodes - num : 0;
         const int j1 = (p->heuristic == 3) ? n_nodes : num;
         uint32_t chunks = 0;
@@ -1121,7 +1130,7 @@ int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit,
       }
     }
   }
-  if (p->second_prefetch) {  // :3645-3683
+  if (p->second_prefetch && !queue_variant) {  // :3645-3683
     bool submit_second = false;
     if (queue == 0 && total_threads > 0 && priority.size() > 1) {
       if (last_prefetched == prefetched_treelet_root && prefetched_treelet_root != NONE) {
@@ -1150,6 +1159,12 @@ int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit,
   st->last_rejected = to_unit(last_rejected);
   st->queue_len = (uint32_t)queue;
   return 0;
+}
+
+// shader.cc:3419-3683, one RT unit, one decision.
+int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
+                           const rt_prefetch_params* p, rt_prefetch_state* st, rt_prefetch_decision* out) {
+  return oracle_prefetch_decide_ex(tl, next_unit, lanes, p, st, out, 0, 0);
 }
 
 }  // extern "C"

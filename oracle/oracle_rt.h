@@ -77,6 +77,15 @@ int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* t
 int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
                            const rt_prefetch_params* p, rt_prefetch_state* state, rt_prefetch_decision* out);
 
+/* The same with two switches: queue_variant 1 runs the copy of the decision
+ * that the pipelined treelet queue uses (shader.cc:3780-3932: no second
+ * prefetch, only the last prefetched treelet suppressed, heuristic 3 sized at
+ * half the treelet); flush 1 clears the queue before a new treelet's chunks
+ * (-flush_prefetch_queue_on_new_treelet). */
+int oracle_prefetch_decide_ex(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
+                              const rt_prefetch_params* p, rt_prefetch_state* state, rt_prefetch_decision* out,
+                              uint32_t queue_variant, uint32_t flush);
+
 /* The RT-unit trace replay of rt_unit_replay (treelet_rt.h), restated with
  * the reference's containers: a std::deque prefetch queue erased in place,
  * per-block vectors of prefetch records classified as gpu-cache.cc:1953-2116

@@ -13,6 +13,10 @@
 // (tl_maps.inc, tl_create.inc, as for pin_treelets).
 //
 // Usage: pin_prefetch <blob file> <max bytes per treelet> <cases file> <out file>
+//                     [<queue variant> <flush>]
+// queue variant 1 runs the pipelined treelet queue's copy of the decision
+// (shader.cc:3780-3932, extracted into pf_decide_queue.inc) instead; flush 1
+// sets -flush_prefetch_queue_on_new_treelet.
 // cases file (uint32 words), per case: heuristic, max_queue, threshold as a
 // float's bits, second_prefetch, last_prefetched, last_prefetched_second,
 // last_rejected (root units or 0xFFFFFFFF), queue_len, lanes, then `lanes`
@@ -55,16 +59,23 @@ class RtUnitStandIn {
   unsigned matches = 0;
   unsigned comparisons = 0;
 
+  bool executing = true;  // the pipelined treelet queue is dispatching its warps
+
   void decide() {
 #include "pf_decide.inc"
+  }
+  void decide_queue() {
+#include "pf_decide_queue.inc"
   }
 };
 
 int main(int argc, char** argv) {
-  if (argc != 5) {
-    fprintf(stderr, "usage: pin_prefetch <blob> <max bytes per treelet> <cases> <out>\n");
+  if (argc != 5 && argc != 7) {
+    fprintf(stderr, "usage: pin_prefetch <blob> <max bytes per treelet> <cases> <out> [<queue variant> <flush>]\n");
     return 2;
   }
+  const bool queue_variant = argc == 7 && atoi(argv[5]) != 0;
+  pin::g_core.cfg.m_flush_prefetch_queue_on_new_treelet = argc == 7 && atoi(argv[6]) != 0;
   const std::vector<uint8_t> raw = read_file(argv[3]);
   if (!load_scene(argv[1], atoi(argv[2])) || raw.size() % 4) return 2;
   std::vector<uint32_t> w(raw.size() / 4);
@@ -95,9 +106,17 @@ int main(int argc, char** argv) {
         warp.threads[k % 32].RT_mem_accesses.push_back({(new_addr_type)(uintptr_t)addr_of(w[i + k])});
     }
     i += lanes;
-    unit.decide();
-    out.push_back(unit.prefetch_mem_access_q.size() - queue_len);
-    for (size_t q = queue_len; q < unit.prefetch_mem_access_q.size(); ++q) {
+    if (queue_variant)
+      unit.decide_queue();
+    else
+      unit.decide();
+    // the carried entries are (0, 0) and stay at the front unless a flush cleared them
+    size_t keep = 0;
+    while (keep < unit.prefetch_mem_access_q.size() && unit.prefetch_mem_access_q[keep].first == 0 &&
+           unit.prefetch_mem_access_q[keep].second == 0)
+      ++keep;
+    out.push_back(unit.prefetch_mem_access_q.size() - keep);
+    for (size_t q = keep; q < unit.prefetch_mem_access_q.size(); ++q) {
       out.push_back(unit.prefetch_mem_access_q[q].first - (new_addr_type)(uintptr_t)g_blob.data());
       out.push_back((unit.prefetch_mem_access_q[q].second - (new_addr_type)(uintptr_t)g_blob.data()) / 64);
     }

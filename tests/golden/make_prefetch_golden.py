@@ -17,6 +17,10 @@ Run from the repository root in a tree where the reference is available:
     make -C oracle/ref_pin REFERENCE=/root/reference
     python tests/golden/make_prefetch_golden.py
 The committed .npz is what tests/test_golden.py checks the oracle against.
+
+The same cases also run through the pipelined treelet queue's copy of the
+decision (shader.cc:3780-3932) and with -flush_prefetch_queue_on_new_treelet
+set: VARIANTS, kept as f"{scene}__q{variant}f{flush}__digests".
 """
 import hashlib
 import os
@@ -36,6 +40,8 @@ NONE = 0xFFFFFFFF
 
 # (scene, budget, cases, seed)
 SCENES = [("kat", 256, 120, 1), ("cube", 1024, 400, 2), ("shared", 512, 300, 3)]
+# (queue variant, flush) beyond the main block without flush
+VARIANTS = [(0, 1), (1, 0), (1, 1)]
 
 
 def scene(name):
@@ -135,7 +141,14 @@ def main():
             cw.tofile(cp)
             subprocess.run([PIN, bp, str(budget), cp, op], check=True, capture_output=True)
             res = np.fromfile(op, np.uint64)
-        per_case = split_results(res, len(cases))
+            per_case = split_results(res, len(cases))
+            for variant, flush in VARIANTS:
+                subprocess.run([PIN, bp, str(budget), cp, op, str(variant), str(flush)], check=True,
+                               capture_output=True)
+                v = split_results(np.fromfile(op, np.uint64), len(cases))
+                arrays[f"{name}__q{variant}f{flush}__digests"] = np.stack([digest(w) for w in v])
+                changed = sum(not np.array_equal(a, b) for a, b in zip(v, per_case))
+                print(f"  {name} variant {variant} flush {flush}: {changed} cases differ from the main block")
         arrays[f"{name}__scene_sha256"] = np.frombuffer(hashlib.sha256(blob.tobytes()).digest(), np.uint8)
         arrays[f"{name}__cases_sha256"] = np.frombuffer(hashlib.sha256(cw.tobytes()).digest(), np.uint8)
         arrays[f"{name}__digests"] = np.stack([digest(w) for w in per_case])

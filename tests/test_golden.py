@@ -202,19 +202,21 @@ def _prefetch_scenes():
     import sys
 
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
-    from make_prefetch_golden import SCENES
+    from make_prefetch_golden import SCENES, VARIANTS
 
-    return SCENES
+    return [s + v for s in SCENES for v in [(0, 0)] + VARIANTS]
 
 
-@pytest.mark.parametrize("name,budget,n_cases,seed", _prefetch_scenes())
-def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases, seed):
+@pytest.mark.parametrize("name,budget,n_cases,seed,variant,flush", _prefetch_scenes())
+def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases, seed, variant, flush):
     """The oracle's treelet-prefetch decision against the reference's own
     decision block (shader.cc:3419-3685, compiled in place by oracle/ref_pin;
     fixtures made by tests/golden/make_prefetch_golden.py): for every case the
     32-byte chunks queued (address and node, in order, for the most popular
     treelet and for the second-prefetch rule) and the carried state after the
-    decision."""
+    decision.  variant 1 checks the pipelined treelet queue's copy of the
+    decision (shader.cc:3780-3932); flush 1 sets
+    -flush_prefetch_queue_on_new_treelet."""
     import hashlib
     import sys
 
@@ -246,7 +248,8 @@ def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases,
         state["last_prefetched"], state["last_prefetched_second"] = c["last_prefetched"], c["last_second"]
         state["last_rejected"], state["queue_len"] = c["last_rejected"], c["queue_len"]
         dec, st = orc.prefetch_decide(tl, c["next_unit"], heuristic=c["heuristic"], max_queue=c["max_queue"],
-                                      threshold=c["threshold"], second_prefetch=bool(c["second"]), state=state)
+                                      threshold=c["threshold"], second_prefetch=bool(c["second"]), state=state,
+                                      queue_variant=bool(variant), flush=bool(flush))
         queued = []
         if dec["submitted"]:
             queued += chunks(int(dec["treelet"]), int(dec["first_member"]),
@@ -257,7 +260,8 @@ def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases,
         words = [len(queued)] + [x for pair in queued for x in pair] + [
             int(st["last_prefetched"]), int(st["last_prefetched_second"]), int(st["last_rejected"]),
             int(st["queue_len"])]
-        if not np.array_equal(digest(np.array(words, np.uint64)), g[f"{name}__digests"][i]):
+        key = f"{name}__digests" if (variant, flush) == (0, 0) else f"{name}__q{variant}f{flush}__digests"
+        if not np.array_equal(digest(np.array(words, np.uint64)), g[key][i]):
             bad.append(i)
     assert not bad, (name, "cases differing from the reference:", bad[:10])
 
