@@ -60,42 +60,87 @@ STAGED_DRAM_BYTES_PER_RAY = {"primary": (103.862784e6 + 16.576000e6) / 262144,
                              "bounce": (171.958528e6 + 33.870336e6) / 262144}
 
 
+# What binds the staged walk, from the same ncu capture (bounce launch): it
+# moves a small fraction of the HBM roofline's bytes, and is bound by SIMT
+# divergence and issue instead.
+LIMITER = {"kind": "issue / SIMT divergence (dependent loads of a pointer-chasing walk), not HBM bandwidth",
+           "source": "profiles/trace_kernels_terrain_instances.md, staged walk, 262,144 bounce rays",
+           "lanes_active_of_32": 9.37, "issue_slots_active_pct": 68.1, "warps_per_sm": 19.9,
+           "dram_busy_pct": 2.2, "l1_hit_pct": 55.1, "l2_hit_pct": 71.1}
+
+
 def _traffic_per_ray():
     """DRAM bytes per ray of the staged kernel, averaged over the primary and bounce launches."""
     return {"staged_dram_bytes_per_ray": (STAGED_DRAM_BYTES_PER_RAY["primary"] + STAGED_DRAM_BYTES_PER_RAY["bounce"]) / 2}
 
 
 REF_WALK = os.path.join(REPO, "oracle", "_ref", "pin_traversal")
+SAMPLE_GEN = os.path.join(REPO, "oracle", "sample_gen")
 
 
-def cpu_walk_seconds(bb: np.ndarray, rays: np.ndarray, threads: int, reps: int):
-    """Seconds per pass of the CPU baseline over `rays` (plain traceRay order,
-    opaque closest hit) on `threads` host threads, `reps` timed passes after
-    an untimed one.  The reference's own traceRay, compiled in place from its
-    sources (oracle/_ref/pin_traversal), when it is built; else the oracle's
-    restatement.  Returns (seconds per pass, kind)."""
+def cpu_walk_files(blob_path: str, rays_path: str, n_rays: int, mode: int, threads: int, reps: int,
+                   hits_out: str | None = None):
+    """Seconds per pass of the CPU baseline over the rays in `rays_path` (opaque
+    closest hit; mode 0 traceRay, 1 traceRayWithTreelets with 8 KiB treelets)
+    on `threads` host threads, `reps` timed passes after an untimed one: the
+    reference's own walk, compiled in place from its sources
+    (oracle/_ref/pin_traversal), when it is built; else the oracle's
+    restatement.  With `hits_out`, the reference's hit words of every ray
+    (11 u32 per ray: hit_geometry, geometry, primitive, instance, t,
+    barycentrics, point) are written there.  Returns (seconds per pass, kind)."""
     if os.path.exists(REF_WALK):
-        import tempfile
-
-        with tempfile.TemporaryDirectory() as d:
-            bp, rp = os.path.join(d, "blob"), os.path.join(d, "rays")
-            bb.tofile(bp)
-            np.ascontiguousarray(rays).tofile(rp)
-            r = subprocess.run([REF_WALK, "--time", bp, rp, "0", "1", str(BUDGET), str(threads), str(reps)],
-                               capture_output=True, text=True, timeout=900)
+        cmd = [REF_WALK, "--time", blob_path, rays_path, str(mode), "1", str(BUDGET), str(threads), str(reps)]
+        if hits_out:
+            cmd.append(hits_out)
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
         secs = [float(ln.split()[2]) for ln in r.stderr.splitlines() if ln.startswith("rep ")]
         if r.returncode == 0 and len(secs) == reps:
             return secs, "reference"
         print(f"reference walk harness failed ({r.returncode}); timing the oracle port", file=sys.stderr)
     from oracle import oracle as orc
 
-    orc.trace(bb, rays[: min(len(rays), 2048)], 0, threads=threads)
+    bb = np.fromfile(blob_path, np.uint8)
+    rays = np.fromfile(rays_path, np.uint8).view(orc.RAY_DTYPE)
+    tl = orc.Treelets(bb, BUDGET) if mode == 1 else None
+    orc.trace(bb, rays[: min(len(rays), 2048)], mode, tl, threads=threads)
     secs = []
     for _ in range(reps):
         t = time.perf_counter()
-        orc.trace(bb, rays, 0, threads=threads)
+        hits, _, _ = orc.trace(bb, rays, mode, tl, threads=threads)
         secs.append(time.perf_counter() - t)
+    if hits_out:
+        _hit_words(hits).tofile(hits_out)
     return secs, "port"
+
+
+def _hit_words(hits: np.ndarray) -> np.ndarray:
+    """Hit records in the reference walk harness's 11-word layout (zeros for a miss)."""
+    w = np.zeros((len(hits), 11), np.uint32)
+    hit = hits["hit_geometry"] != 0
+    w[:, 0] = hit
+    w[:, 1] = hits["geometry_index"]
+    w[:, 2] = hits["primitive_index"]
+    w[:, 3] = hits["instance_index"]
+    w[:, 4] = hits["world_min_thit"].view(np.uint32)
+    w[:, 5:8] = hits["barycentric"].view(np.uint32)
+    w[:, 8:11] = hits["intersection_point"].view(np.uint32)
+    w[~hit] = 0
+    return w
+
+
+def cpu_walk_seconds(bb: np.ndarray, rays: np.ndarray, threads: int, reps: int, mode: int = 0,
+                     want_hits: bool = False):
+    """cpu_walk_files over in-memory arrays (written to a temporary folder);
+    returns (seconds per pass, kind, hit words or None)."""
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as d:
+        bp, rp, hp = os.path.join(d, "blob"), os.path.join(d, "rays"), os.path.join(d, "hits")
+        bb.tofile(bp)
+        np.ascontiguousarray(rays).tofile(rp)
+        secs, kind = cpu_walk_files(bp, rp, len(rays), mode, threads, reps, hp if want_hits else None)
+        words = np.fromfile(hp, np.uint32).reshape(-1, 11) if want_hits else None
+    return secs, kind, words
 
 
 class ClockSampler:
@@ -184,35 +229,60 @@ def run_reference(args, rank: int, world: int) -> None:
     """The reference's CPU traceRay on the host cores, all threads, over a
     bounded sample of the same workload per step: the reference's own code
     compiled in place from its sources (oracle/_ref/pin_traversal) when it is
-    built, else the oracle's line-by-line restatement."""
-    import treelet_rt as rt
-    from oracle import oracle as orc
+    built, else the oracle's line-by-line restatement.  The sample's scene and
+    rays come from oracle/sample_gen, a separate program, so this process
+    loads none of the library's shared objects; a single-thread pass over a
+    smaller slice is reported beside the all-core number."""
+    import tempfile
 
     if rank != 0:
         return
-    blob, prim, _ = make_workload(False)
-    bb = blob.bytes()
     threads = os.cpu_count() or 1
-    n_prim = len(prim)
-    idx = np.linspace(0, n_prim - 1, args.ref_step_rays // 2).astype(np.int64)
-    ps = prim[idx]
-    ph, _, _ = orc.trace(bb, ps, 0, threads=threads)
-    bounce = rt.bounce_rays_host(blob, ps, ph, seed=SEED + 100)
-    rays = np.concatenate([ps, bounce])
-    secs, kind = cpu_walk_seconds(bb, rays, threads, args.steps)
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run([SAMPLE_GEN, d, str(WIDTH), str(HEIGHT), str(SPP), str(SEED), str(args.ref_step_rays),
+                            str(threads)], capture_output=True, text=True, timeout=900)
+        if r.returncode != 0:
+            print(json.dumps({"impl": "reference", "unavailable": f"sample_gen failed: {r.stderr.strip()[-200:]}"}))
+            return
+        n_prim, n_bounce = (int(x) for x in r.stdout.split())
+        bp, rp = os.path.join(d, "blob"), os.path.join(d, "rays")
+        n_rays = n_prim + n_bounce
+        secs, kind = cpu_walk_files(bp, rp, n_rays, 0, threads, args.steps)
+        # single thread, over every 16th ray of the sample
+        rays = np.fromfile(rp, np.uint8).reshape(-1, 32)
+        one = rays[::16]
+        rp1 = os.path.join(d, "rays1")
+        one.tofile(rp1)
+        secs1, _ = cpu_walk_files(bp, rp1, len(one), 0, 1, 1)
     total = sum(secs)
-    v = len(rays) * args.steps / total / 1e6
+    v = n_rays * args.steps / total / 1e6
+    v1 = len(one) / secs1[0] / 1e6
+    sample = (f"{n_rays} rays per step: {n_prim} primary rays spread over the frame + their {n_bounce} bounce "
+              f"rays; single thread: every 16th of them ({len(one)} rays)")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_rays_per_step": int(len(rays)), "mode": "traceRay (plain)"},
-        "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": kind,
-                         "sample": f"{len(rays)} rays per step: {len(ps)} primary rays spread over the frame + "
-                                   f"their {len(bounce)} bounce rays"},
+        "config": {"workload": WORKLOAD, "sample_rays_per_step": int(n_rays), "mode": "traceRay (plain)"},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": kind, "sample": sample,
+                         "single_thread": {"value": round(v1, 4), "unit": "Mrays/s", "cores": 1}},
         "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+TRACE_CAP = 256  # trace entries per ray of the traced timings (visit and treelet-id rows)
+
+
+def _gpu_words(d_hits, idx) -> np.ndarray:
+    """The hit records of rays `idx` of a device hit buffer, in the reference
+    walk harness's 11-word layout."""
+    import torch
+
+    import treelet_rt as rt
+
+    rows = d_hits.view(-1, 64)[torch.as_tensor(idx, device=d_hits.device)]
+    return _hit_words(np.frombuffer(rows.cpu().numpy().tobytes(), rt.HIT_DTYPE))
 
 
 def run_gpu(args, rank: int, world: int) -> None:
@@ -240,11 +310,12 @@ def run_gpu(args, rank: int, world: int) -> None:
     n_prim = len(prim)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    d_prim = torch.from_numpy(prim.view(np.uint8)).to(f"cuda:{dev}")
-    d_hits_p = torch.empty(n_prim * 64, dtype=torch.uint8, device=f"cuda:{dev}")
-    d_bounce = torch.empty(n_prim * 32, dtype=torch.uint8, device=f"cuda:{dev}")
-    d_hits_b = torch.empty(n_prim * 64, dtype=torch.uint8, device=f"cuda:{dev}")
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    cuda = f"cuda:{dev}"
+    d_prim = torch.from_numpy(prim.view(np.uint8)).to(cuda)
+    d_hits_p = torch.empty(n_prim * 64, dtype=torch.uint8, device=cuda)
+    d_bounce = torch.empty(n_prim * 32, dtype=torch.uint8, device=cuda)
+    d_hits_b = torch.empty(n_prim * 64, dtype=torch.uint8, device=cuda)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=cuda)
     with torch.cuda.stream(stream):
         scene.trace(d_prim, d_hits_p, rt.MODE_PLAIN, stream=sp, n=n_prim)
         scene.bounce(d_prim, d_hits_p, d_bounce, seed=SEED + 100, stream=sp, n=n_prim)
@@ -253,17 +324,26 @@ def run_gpu(args, rank: int, world: int) -> None:
     hit_rate = float(np.frombuffer(d_hits_p.cpu().numpy().tobytes(), rt.HIT_DTYPE)["hit_geometry"].mean())
 
     names = {rt.MODE_PLAIN: "plain", rt.MODE_TREELET: "treelet", rt.MODE_STAGED: "staged"}
+    # visit and treelet-id rows for the traced timings (the access trace the
+    # reference hands to its timing model with every traced ray)
+    d_vis = torch.empty(n_prim * TRACE_CAP, dtype=torch.int32, device=cuda)
+    d_tl = torch.empty(n_prim * TRACE_CAP, dtype=torch.int32, device=cuda)
 
-    def step(mode):
-        apply_tuning(scene, names[mode], "primary")
-        scene.trace(d_prim, d_hits_p, mode, stream=sp, n=n_prim)
-        apply_tuning(scene, names[mode], "bounce")
-        scene.trace(d_bounce, d_hits_b, mode, stream=sp, n=n_prim)
+    def launch(mode, rays_d, hits_d, batch, traced):
+        apply_tuning(scene, names[mode], batch)
+        if traced:
+            scene.trace(rays_d, hits_d, mode, visits=d_vis, treelets=d_tl, capacity=TRACE_CAP, stream=sp, n=n_prim)
+        else:
+            scene.trace(rays_d, hits_d, mode, stream=sp, n=n_prim)
 
-    def timed(mode, steps, warmup, per_batch=False):
+    def step(mode, traced=False):
+        launch(mode, d_prim, d_hits_p, "primary", traced)
+        launch(mode, d_bounce, d_hits_b, "bounce", traced)
+
+    def timed(mode, steps, warmup, traced=False):
         for _ in range(warmup):
             with torch.cuda.stream(stream):
-                step(mode)
+                step(mode, traced)
         stream.synchronize()
         ms, ms_p, ms_b = [], [], []
         for _ in range(steps):
@@ -272,10 +352,9 @@ def run_gpu(args, rank: int, world: int) -> None:
                 e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
                 apply_tuning(scene, names[mode], "primary")
                 e0.record(stream)
-                scene.trace(d_prim, d_hits_p, mode, stream=sp, n=n_prim)
+                launch(mode, d_prim, d_hits_p, "primary", traced)
                 e1.record(stream)
-                apply_tuning(scene, names[mode], "bounce")
-                scene.trace(d_bounce, d_hits_b, mode, stream=sp, n=n_prim)
+                launch(mode, d_bounce, d_hits_b, "bounce", traced)
                 e2.record(stream)
             stream.synchronize()
             ms.append(e0.elapsed_time(e2))
@@ -283,7 +362,12 @@ def run_gpu(args, rank: int, world: int) -> None:
             ms_b.append(e1.elapsed_time(e2))
         return ms, ms_p, ms_b
 
-    # correctness guard: staged hits must equal plain-order treelet hits
+    def rates(ms, msp, msb, prefix=""):
+        return {prefix + "mrays_s": n_rays / (sum(ms) / len(ms)) / 1e3,
+                prefix + "primary_mrays_s": n_prim / (sum(msp) / len(msp)) / 1e3,
+                prefix + "bounce_mrays_s": n_prim / (sum(msb) / len(msb)) / 1e3}
+
+    # correctness guard: staged hits must equal treelet-order hits on the full batch
     with torch.cuda.stream(stream):
         scene.trace(d_prim, d_hits_p, rt.MODE_TREELET, stream=sp, n=n_prim)
     stream.synchronize()
@@ -292,13 +376,11 @@ def run_gpu(args, rank: int, world: int) -> None:
         scene.trace(d_prim, d_hits_p, rt.MODE_STAGED, stream=sp, n=n_prim)
     stream.synchronize()
     staged_exact = bool(torch.equal(ref_hits, d_hits_p))
+    del ref_hits
 
     results = {}
     for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET)):
-        ms, msp, msb = timed(mode, max(3, args.steps // 2), args.warmup)
-        results[name] = {"mrays_s": n_rays / (sum(ms) / len(ms)) / 1e3,
-                         "primary_mrays_s": n_prim / (sum(msp) / len(msp)) / 1e3,
-                         "bounce_mrays_s": n_prim / (sum(msb) / len(msb)) / 1e3}
+        results[name] = rates(*timed(mode, max(3, args.steps // 2), args.warmup))
 
     # headline: staged, with clocks sampled during the timed region
     if dist:
@@ -311,65 +393,100 @@ def run_gpu(args, rank: int, world: int) -> None:
     torch.cuda.synchronize()
     stats = scene.stats()  # counters of the last staged launch (bounce batch)
     with torch.cuda.stream(stream):
-        scene.trace(d_prim, d_hits_p, rt.MODE_STAGED, stream=sp, n=n_prim)
+        launch(rt.MODE_STAGED, d_prim, d_hits_p, "primary", False)
     stream.synchronize()
     stats_p = scene.stats()
     total_ms = sum(ms)
     t_local = total_ms / 1e3
     if dist:
-        t = torch.tensor([t_local], device=f"cuda:{dev}")
+        t = torch.tensor([t_local], device=cuda)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_local = float(t.item())
     value = n_rays * args.steps * world / t_local / 1e6
-    results["staged"] = {"mrays_s": n_rays / (total_ms / len(ms)) / 1e3,
-                         "primary_mrays_s": n_prim / (sum(msp) / len(msp)) / 1e3,
-                         "bounce_mrays_s": n_prim / (sum(msb) / len(msb)) / 1e3}
+    results["staged"] = rates(ms, msp, msb)
 
-    # roofline of the dominant kernel (staged traversal), per launch (one batch)
+    # traced timings: every mode writing its visit and treelet-id rows
+    for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
+        results[name].update(rates(*timed(mode, max(3, args.steps // 4), 1, traced=True), prefix="traced_"))
+
+    # roofline of the dominant kernel (the staged walk): algorithmic bytes
+    # (the node transactions of its visit traces plus ray and hit) over kernel
+    # time, per launch and over the whole step
     peak, peak_kind = _peaks()
     alg_p = stats_p["node_bytes"] + n_prim * (32 + 64)
     alg_b = stats["node_bytes"] + n_prim * (32 + 64)
-    achieved = ((alg_p / (sum(msp) / len(msp)) + alg_b / (sum(msb) / len(msb))) / 2) / 1e6  # GB/s
-    traffic = _traffic_per_ray()
-    traffic_launch = None
-    if traffic and "staged_dram_bytes_per_ray" in traffic:
-        traffic_launch = int(traffic["staged_dram_bytes_per_ray"] * n_prim)
+    t_p, t_b = sum(msp) / len(msp), sum(msb) / len(msb)
+    achieved = (alg_p + alg_b) / (t_p + t_b) / 1e6  # GB/s
+    traffic_launch = int(_traffic_per_ray()["staged_dram_bytes_per_ray"] * n_prim)
+    dram_gbs = {"primary": round(STAGED_DRAM_BYTES_PER_RAY["primary"] * n_prim / t_p / 1e6, 1),
+                "bounce": round(STAGED_DRAM_BYTES_PER_RAY["bounce"] * n_prim / t_b / 1e6, 1)}
 
-    # end to end through the C ABI with host buffers (pinned)
+    # end to end through the C ABI with host buffers (page-locked): hit records
+    # only, and with the visit and treelet-id rows copied back as well
     h_prim = torch.from_numpy(prim.view(np.uint8)).pin_memory()
     h_bounce = d_bounce.cpu().pin_memory()
     h_hits = torch.empty(n_prim * 64, dtype=torch.uint8).pin_memory()
-    from treelet_rt._ffi import check, lib
+    from treelet_rt._ffi import TraceBuf, check, lib
 
-    def host_trace(hr, batch):
+    def host_trace(hr, batch, tb=None):
         apply_tuning(scene, "staged", batch)
         check(lib().rt_trace_host(scene.handle, hr.data_ptr(), None, rt.RAY_FLAG_OPAQUE, n_prim, rt.MODE_STAGED,
-                                  h_hits.data_ptr(), None))
+                                  h_hits.data_ptr(), tb))
 
-    for _ in range(max(1, args.warmup)):  # both batches, so every host buffer is touched first
-        host_trace(h_prim, "primary")
-        host_trace(h_bounce, "bounce")
-    e2e_t = []
-    for _ in range(max(3, args.steps // 2)):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        host_trace(h_prim, "primary")
-        host_trace(h_bounce, "bounce")
-        e2e_t.append(time.perf_counter() - t)
-    e2e = n_rays / (sum(e2e_t) / len(e2e_t)) / 1e6 * world
+    def e2e_rate(tb, reps):
+        for _ in range(max(1, args.warmup)):  # both batches, so every host buffer is touched first
+            host_trace(h_prim, "primary", tb)
+            host_trace(h_bounce, "bounce", tb)
+        tt = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            host_trace(h_prim, "primary", tb)
+            host_trace(h_bounce, "bounce", tb)
+            tt.append(time.perf_counter() - t)
+        return n_rays / (sum(tt) / len(tt)) / 1e6 * world
 
-    # CPU baseline: oracle traceRay on a bounded sample, all host threads
-    # CPU baseline: the reference's traceRay on a bounded sample, all host threads
+    e2e = e2e_rate(None, max(3, args.steps // 2))
+    h_vis = torch.empty(n_prim * TRACE_CAP, dtype=torch.int32).pin_memory()
+    h_tl = torch.empty(n_prim * TRACE_CAP, dtype=torch.int32).pin_memory()
+    tb = TraceBuf(h_vis.data_ptr(), h_tl.data_ptr(), TRACE_CAP)
+    import ctypes
+
+    e2e_traced = e2e_rate(ctypes.byref(tb), 3)
+    del h_vis, h_tl
+
+    # CPU baseline and parity sample: the reference's own traceRay over a
+    # bounded sample of the same rays (primary rays spread over the frame and
+    # their bounce rays), all host threads, with its hit records compared bit
+    # for bit against the GPU's; traceRayWithTreelets over every 8th of them
+    # against the treelet-order and staged walks; one thread over every 16th.
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         idx = np.linspace(0, n_prim - 1, args.ref_sample // 2).astype(np.int64)
         hb = np.frombuffer(d_bounce.cpu().numpy().tobytes(), rt.RAY_DTYPE)
         sample = np.concatenate([prim[idx], hb[idx]])
-        secs, kind = cpu_walk_seconds(blob.bytes(), sample, threads, 1)
+        bb = blob.bytes()
+        secs, kind, ref_w = cpu_walk_seconds(bb, sample, threads, 1, mode=0, want_hits=True)
+        idx_t = idx[::8]
+        sample_t = np.concatenate([prim[idx_t], hb[idx_t]])
+        _, kind_t, ref_wt = cpu_walk_seconds(bb, sample_t, threads, 1, mode=1, want_hits=True)
+        secs1, _, _ = cpu_walk_seconds(bb, sample[::16], 1, 1)
+        parity = {"rays": int(len(sample)), "treelet_rays": int(len(sample_t)), "reference_kind": kind,
+                  "mismatches": {}}
+        for name, mode, rw, ix in (("plain", rt.MODE_PLAIN, ref_w, idx), ("treelet", rt.MODE_TREELET, ref_wt, idx_t),
+                                   ("staged", rt.MODE_STAGED, ref_wt, idx_t)):
+            with torch.cuda.stream(stream):
+                step(mode)
+            stream.synchronize()
+            got = np.concatenate([_gpu_words(d_hits_p, ix), _gpu_words(d_hits_b, ix)])
+            parity["mismatches"][name] = int((got != rw).any(axis=1).sum())
         cpu = {"value": round(len(sample) / secs[0] / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": kind,
-               "sample": f"{len(sample)} rays: {len(idx)} primary rays spread over the frame + their bounce rays"}
+               "sample": f"{len(sample)} rays: {len(idx)} primary rays spread over the frame + their bounce rays",
+               "single_thread": {"value": round(len(sample[::16]) / secs1[0] / 1e6, 4), "unit": "Mrays/s",
+                                 "cores": 1, "sample": f"every 16th ray of the sample ({len(sample[::16])} rays)"}}
 
     if rank == 0:
         line = {
@@ -378,7 +495,7 @@ def run_gpu(args, rank: int, world: int) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "mode": "staged (treelet order, smem staging)", "l2": "flushed",
                        "treelets": int(tinfo["n_treelets"]), "blob_bytes": int(blob.nbytes()),
-                       "primary_hit_rate": round(hit_rate, 4),
+                       "primary_hit_rate": round(hit_rate, 4), "trace_capacity": TRACE_CAP,
                        "tuning": {b: apply_tuning(scene, "staged", b) or scene.get_tuning()
                                   for b in ("primary", "bounce")},
                        "setup_s": {"scene_gen": round(t_gen, 2), "treelets": round(t_form, 2)}},
@@ -388,12 +505,23 @@ def run_gpu(args, rank: int, world: int) -> None:
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic_launch,
                          "peak_source": f"{peak_kind} hbm_gbs",
-                         "algorithmic_bytes_per_launch": {"primary": int(alg_p), "bounce": int(alg_b)}},
+                         "achieved_is": "algorithmic bytes (node transactions + ray + hit) / kernel time, both "
+                                        "launches of the step",
+                         "per_launch": {"primary": {"bytes": int(alg_p), "ms": round(t_p, 4),
+                                                    "frac": round(alg_p / t_p / 1e6 / peak, 4)},
+                                        "bounce": {"bytes": int(alg_b), "ms": round(t_b, 4),
+                                                   "frac": round(alg_b / t_b / 1e6 / peak, 4)}},
+                         "dram_gbs": dram_gbs,
+                         "limiter": LIMITER},
             "e2e": {"value": round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n_rays * 32,
-                    "d2h_bytes_per_step": n_rays * 64},
+                    "d2h_bytes_per_step": n_rays * 64,
+                    "traced": {"value": round(e2e_traced, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n_rays * 32,
+                               "d2h_bytes_per_step": n_rays * (64 + 2 * 4 * TRACE_CAP)}},
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,
         }
+        if parity:
+            line["parity_sample"] = parity
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

@@ -299,6 +299,9 @@ typedef struct rt_tuning {
   uint32_t staged_min_votes;  /* lanes of a warp that must want a treelet to stage it (1..32) */
   uint32_t stack_depth;       /* traversal stack entries per ray: 48, 96 or 160 (deeper rays are flagged) */
   uint32_t pinned_bytes;      /* shared memory per CTA for pinned treelets (256..229376; RT_TUNING_OFF: none) */
+  uint32_t wait_tries;        /* probes of a CTA's wait for its pinned treelets before it stops staging
+                                 (1..2^24; the first probe does not block); the wait for copies still in
+                                 flight when a CTA exits always keeps the default limit (2^22) */
 } rt_tuning;
 rt_status rt_scene_set_tuning(rt_scene* scene, const rt_tuning* t);
 rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);

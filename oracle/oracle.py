@@ -64,6 +64,9 @@ def lib():
         L.oracle_trace.restype = C.c_int
         L.oracle_trace.argtypes = [vp, C.c_uint64, vp, vp, vp, C.c_uint32, C.c_uint64, C.c_int, vp, vp, vp,
                                    C.c_uint32, C.c_int]
+        L.oracle_trace_peaks.restype = C.c_int
+        L.oracle_trace_peaks.argtypes = [vp, C.c_uint64, vp, vp, vp, C.c_uint32, C.c_uint64, C.c_int, vp, vp, vp,
+                                         C.c_uint32, vp, C.c_int]
         L.oracle_prefetch_decide.restype = C.c_int
         L.oracle_prefetch_decide.argtypes = [vp, vp, C.c_uint32, C.POINTER(_Params), vp, vp]
         L.oracle_prefetch_decide_ex.restype = C.c_int
@@ -174,6 +177,28 @@ def trace(blob: np.ndarray, rays: np.ndarray, mode: int = 0, treelets: Treelets 
     if rc != 0:
         raise OracleError(lib().oracle_last_error().decode())
     return hits, vis, tl
+
+
+def stack_peaks(blob: np.ndarray, rays: np.ndarray, mode: int = 0, treelets: Treelets | None = None, flags=None,
+                default_flags: int = 1, threads: int = 1):
+    """Hits and, per ray, the largest sizes the reference's stacks reached: (n, 2) uint32, traceRay's
+    stack and 0 (mode 0), or the current- and other-treelet stacks (modes 1, 2)."""
+    blob = np.ascontiguousarray(blob, np.uint8)
+    if treelets is not None:
+        if blob.nbytes != treelets.blob.nbytes or not np.array_equal(blob, treelets.blob):
+            raise OracleError("stack_peaks: blob differs from the one the treelets were formed on")
+        blob = treelets.blob
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    n = len(rays)
+    hits = np.zeros(n, HIT_DTYPE)
+    peaks = np.zeros((n, 2), np.uint32)
+    fl = None if flags is None else np.ascontiguousarray(flags, np.uint32)
+    rc = lib().oracle_trace_peaks(blob.ctypes.data, blob.nbytes, treelets.h if treelets else None, rays.ctypes.data,
+                                  fl.ctypes.data if fl is not None else None, default_flags, n, mode,
+                                  hits.ctypes.data, None, None, 0, peaks.ctypes.data, threads)
+    if rc != 0:
+        raise OracleError(lib().oracle_last_error().decode())
+    return hits, peaks
 
 
 def unit_replay(treelets: Treelets, hits: np.ndarray, visits: np.ndarray, config, threads: int = 8) -> np.ndarray:

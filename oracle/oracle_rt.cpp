@@ -475,6 +475,12 @@ inline uint32_t unit_of(const uint8_t* base, const uint8_t* a) { return (uint32_
 struct TraceOut {
   std::vector<Tx> transactions;
   rt_hit hit{};
+  // Largest stack sizes the walk reached: traceRay's one stack (peak[0]),
+  // or the current / other treelet stacks of traceRayWithTreelets
+  // (peak[0] / peak[1]).  Not part of the reference's output; the tests use
+  // them to predict which rays exceed a bounded stack.
+  uint32_t peak[2] = {0, 0};
+  void note(uint32_t k, size_t size) { peak[k] = std::max<uint32_t>(peak[k], (uint32_t)size); }
 };
 
 void finish_hit(TraceOut& o, bool hit, float min_thit, const Ray& ray, const GEN_RT_BVH_QUAD_LEAF& closest_leaf,
@@ -529,7 +535,7 @@ void trace_plain(const uint8_t* tlas, uint32_t rayFlags, float3 origin, float Tm
     float thit;
     if (ray_box_test(topBVH.BoundsMin, topBVH.BoundsMax, calculate_idir(ray.get_direction()), ray.get_origin(),
                      ray.get_tmin(), ray.get_tmax(), thit))
-      stack.push_back(StackEntry(topRootAddr, true, false));
+      { stack.push_back(StackEntry(topRootAddr, true, false)); out.note(0, stack.size()); }
   }
   while (!stack.empty()) {  // :2486
     const uint8_t* next_node_addr = nullptr;
@@ -559,11 +565,11 @@ void trace_plain(const uint8_t* tlas, uint32_t rayFlags, float3 origin, float Tm
       for (int i = 0; i < 6; i++) {
         if (child_hit[i]) {
           if (node.ChildType[i] != NODE_TYPE_INTERNAL)
-            stack.push_back(StackEntry(child_addr, true, true));
+            { stack.push_back(StackEntry(child_addr, true, true)); out.note(0, stack.size()); }
           else if (next_node_addr == nullptr)
             next_node_addr = child_addr;
           else
-            stack.push_back(StackEntry(child_addr, true, false));
+            { stack.push_back(StackEntry(child_addr, true, false)); out.note(0, stack.size()); }
         }
         child_addr += node.ChildSize[i] * 64;
       }
@@ -581,7 +587,7 @@ void trace_plain(const uint8_t* tlas, uint32_t rayFlags, float3 origin, float Tm
       transactions.push_back({blasHdr, RT_TX_STRUCTURE});
       float worldToObject_tMultiplier;
       Ray objectRay = make_transformed_ray(ray, worldToObjectMatrix, &worldToObject_tMultiplier);
-      stack.push_back(StackEntry(blasHdr + botLevelASAddr.RootNodeOffset, false, false));
+      { stack.push_back(StackEntry(blasHdr + botLevelASAddr.RootNodeOffset, false, false)); out.note(0, stack.size()); }
       while (!stack.empty() && !stack.back().topLevel) {  // :2679
         const uint8_t* nnext = stack.back().addr;
         stack.pop_back();
@@ -608,11 +614,11 @@ void trace_plain(const uint8_t* tlas, uint32_t rayFlags, float3 origin, float Tm
           for (int i = 0; i < 6; i++) {
             if (child_hit[i]) {
               if (node.ChildType[i] != NODE_TYPE_INTERNAL)
-                stack.push_back(StackEntry(child_addr, false, true));
+                { stack.push_back(StackEntry(child_addr, false, true)); out.note(0, stack.size()); }
               else if (nnext == nullptr)
                 nnext = child_addr;
               else
-                stack.push_back(StackEntry(child_addr, false, false));
+                { stack.push_back(StackEntry(child_addr, false, false)); out.note(0, stack.size()); }
             }
             child_addr += node.ChildSize[i] * 64;
           }
@@ -693,13 +699,18 @@ void trace_treelets(const uint8_t* tlas, const oracle_treelets& T, uint32_t rayF
         current_treelet_stack.push_back(StackEntry(topRootAddr, true, false));
       else
         other_treelet_stack.push_back(StackEntry(topRootAddr, true, false));
+      out.note(0, current_treelet_stack.size());
+      out.note(1, other_treelet_stack.size());
     }
   }
   auto route = [&](const StackEntry& e) {
-    if (root_is_device_address && current_treelet_root == T.addrToTreeletID(e.addr))
+    if (root_is_device_address && current_treelet_root == T.addrToTreeletID(e.addr)) {
       current_treelet_stack.push_front(e);
-    else
+      out.note(0, current_treelet_stack.size());
+    } else {
       other_treelet_stack.push_front(e);
+      out.note(1, other_treelet_stack.size());
+    }
   };
   while (!current_treelet_stack.empty() || !other_treelet_stack.empty()) {  // :1740
     if (current_treelet_stack.empty()) {  // :1748-1754
@@ -823,10 +834,11 @@ void trace_treelets(const uint8_t* tlas, const oracle_treelets& T, uint32_t rayF
 
 void trace_range(const uint8_t* blob, const oracle_treelets* tl, const rt_ray* rays, const uint32_t* flags,
                  uint32_t default_flags, uint64_t begin, uint64_t end, int mode, rt_hit* hits, uint32_t* visits,
-                 uint32_t* treelets, uint32_t capacity) {
+                 uint32_t* treelets, uint32_t capacity, uint32_t* peaks) {
   TraceOut o;
   for (uint64_t r = begin; r < end; ++r) {
     o.transactions.clear();
+    o.peak[0] = o.peak[1] = 0;
     const rt_ray& ry = rays[r];
     const uint32_t f = flags ? flags[r] : default_flags;
     const float3 org = {ry.origin[0], ry.origin[1], ry.origin[2]};
@@ -837,6 +849,10 @@ void trace_range(const uint8_t* blob, const oracle_treelets* tl, const rt_ray* r
       trace_treelets(blob, *tl, f, org, ry.tmin, dir, ry.tmax, o, mode == 2);
     if (capacity && o.transactions.size() > capacity) o.hit.status |= RT_RAY_TRACE_OVERFLOW;
     hits[r] = o.hit;
+    if (peaks) {
+      peaks[2 * r] = o.peak[0];
+      peaks[2 * r + 1] = o.peak[1];
+    }
     const size_t m = std::min<size_t>(o.transactions.size(), capacity);
     for (size_t j = 0; j < m; ++j) {
       const Tx& t = o.transactions[j];
@@ -1023,6 +1039,13 @@ int oracle_remap(const oracle_treelets* t, int max_bytes, uint32_t stride, uint6
 int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* tl, const rt_ray* rays,
                  const uint32_t* flags, uint32_t default_flags, uint64_t n, int mode, rt_hit* hits, uint32_t* visits,
                  uint32_t* treelets, uint32_t capacity, int threads) {
+  return oracle_trace_peaks(blob, n_bytes, tl, rays, flags, default_flags, n, mode, hits, visits, treelets, capacity,
+                            nullptr, threads);
+}
+
+int oracle_trace_peaks(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* tl, const rt_ray* rays,
+                       const uint32_t* flags, uint32_t default_flags, uint64_t n, int mode, rt_hit* hits,
+                       uint32_t* visits, uint32_t* treelets, uint32_t capacity, uint32_t* peaks, int threads) {
   (void)n_bytes;
   if (mode < 0 || mode > 2) {
     g_err = "oracle_trace: mode must be 0, 1 or 2";
@@ -1034,14 +1057,15 @@ int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* t
   }
   if (!visits && !treelets) capacity = 0;
   if (threads <= 1 || n < 256) {
-    trace_range(blob, tl, rays, flags, default_flags, 0, n, mode, hits, visits, treelets, capacity);
+    trace_range(blob, tl, rays, flags, default_flags, 0, n, mode, hits, visits, treelets, capacity, peaks);
     return 0;
   }
   std::vector<std::thread> th;
   const uint64_t chunk = (n + threads - 1) / threads;
   for (int t = 0; t < threads; ++t) {
     const uint64_t b = std::min<uint64_t>(n, t * chunk), e = std::min<uint64_t>(n, b + chunk);
-    th.emplace_back(trace_range, blob, tl, rays, flags, default_flags, b, e, mode, hits, visits, treelets, capacity);
+    th.emplace_back(trace_range, blob, tl, rays, flags, default_flags, b, e, mode, hits, visits, treelets, capacity,
+                    peaks);
   }
   for (auto& x : th) x.join();
   return 0;

@@ -70,6 +70,15 @@ int oracle_trace(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* t
                  const uint32_t* flags, uint32_t default_flags, uint64_t n, int mode, rt_hit* hits, uint32_t* visits,
                  uint32_t* treelets, uint32_t capacity, int threads);
 
+/* oracle_trace that also writes, per ray, the largest sizes its stacks
+ * reached (peaks[2 r], peaks[2 r + 1]): traceRay's stack and 0, or
+ * traceRayWithTreelets' current-treelet and other-treelet stacks.  The
+ * reference's lists are unbounded; the tests use these sizes to predict which
+ * rays exceed the library's bounded stacks.  peaks may be NULL. */
+int oracle_trace_peaks(const uint8_t* blob, uint64_t n_bytes, const oracle_treelets* tl, const rt_ray* rays,
+                       const uint32_t* flags, uint32_t default_flags, uint64_t n, int mode, rt_hit* hits,
+                       uint32_t* visits, uint32_t* treelets, uint32_t capacity, uint32_t* peaks, int threads);
+
 /* Treelet-prefetch decision of one RT unit (shader.cc:3419-3633 and the
  * second-treelet step :3645-3683).  next_unit holds each resident lane's next
  * access (unit index) or 0xFFFFFFFF.  State and decision use the library's

@@ -26,7 +26,7 @@
 // (root unit of addrToTreeletID(address), or 0xFFFFFFFF in traceRay).
 //
 // Timing: pin_traversal --time <blob> <rays> <mode> <ray flags> <treelet bytes>
-//                              <threads> <reps>   (see time_walk)
+//                              <threads> <reps> [<hits out>]   (see time_walk)
 #include <algorithm>
 #include <atomic>
 #include <cassert>
@@ -313,9 +313,13 @@ uint32_t bits(float f) {
 // "rep <i> <seconds>" per pass on stderr.  The first ray is traced alone
 // first, so that the walk's lazy one-time set-up (createTreelets, the world
 // bounds) is done before the threads start.
-int time_walk(int mode, uint32_t flags, const std::vector<uint8_t>& rays, int threads, int reps) {
+// With `hits_out`, one more untimed pass writes each ray's 11 hit words (the
+// layout of the result file below, without the transactions) there.
+int time_walk(int mode, uint32_t flags, const std::vector<uint8_t>& rays, int threads, int reps,
+              const char* hits_out) {
   uint8_t* tlas = g_blob.data();
   const size_t n = rays.size() / 32;
+  std::vector<uint32_t> words;
   auto trace_range = [&](size_t lo, size_t hi) {
     for (size_t r = lo; r < hi; ++r) {
       float v[8];
@@ -326,6 +330,19 @@ int time_walk(int mode, uint32_t flags, const std::vector<uint8_t>& rays, int th
         VulkanRayTracing::traceRay(tlas, flags, 0xFF, 0, 0, 0, o, v[3], d, v[7], 0, nullptr, &thread);
       else
         VulkanRayTracing::traceRayWithTreelets(tlas, flags, 0xFF, 0, 0, 0, o, v[3], d, v[7], 0, nullptr, &thread);
+      if (!words.empty()) {
+        Traversal_data td;
+        memcpy(&td, thread.mem.last.data(), sizeof td);
+        const Hit_data& h = td.closest_hit;
+        uint32_t* w = words.data() + 11 * r;
+        if (td.hit_geometry) {
+          const uint32_t x[11] = {1u, h.geometry_index, h.primitive_index, h.instance_index, bits(h.world_min_thit),
+                                  bits(h.barycentric_coordinates.x), bits(h.barycentric_coordinates.y),
+                                  bits(h.barycentric_coordinates.z), bits(h.intersection_point.x),
+                                  bits(h.intersection_point.y), bits(h.intersection_point.z)};
+          memcpy(w, x, sizeof x);
+        }
+      }
     }
   };
   trace_range(0, std::min<size_t>(1, n));
@@ -338,12 +355,23 @@ int time_walk(int mode, uint32_t flags, const std::vector<uint8_t>& rays, int th
     const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (rep >= 0) fprintf(stderr, "rep %d %.6f\n", rep, s);
   }
+  if (hits_out) {
+    words.assign(11 * n, 0u);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+      pool.emplace_back(trace_range, n * t / threads, n * (t + 1) / threads);
+    for (auto& th : pool) th.join();
+    FILE* f = fopen(hits_out, "wb");
+    if (!f) return 2;
+    fwrite(words.data(), sizeof(uint32_t), words.size(), f);
+    fclose(f);
+  }
   return 0;
 }
 
 int main(int argc, char** argv) {
-  if (argc == 9 && std::string(argv[1]) == "--time") {
-    // pin_traversal --time <blob> <rays> <mode> <ray flags> <treelet bytes> <threads> <reps>
+  if ((argc == 9 || argc == 10) && std::string(argv[1]) == "--time") {
+    // pin_traversal --time <blob> <rays> <mode> <ray flags> <treelet bytes> <threads> <reps> [<hits out>]
     g_blob = read_file(argv[2]);
     const std::vector<uint8_t> rays = read_file(argv[3]);
     const int mode = atoi(argv[4]);
@@ -357,7 +385,7 @@ int main(int argc, char** argv) {
     find_blases(top.RootNodeOffset, 0);
     if (!freopen("/dev/null", "w", stdout)) return 2;
     std::cout.setstate(std::ios::failbit);
-    return time_walk(mode, (uint32_t)strtoul(argv[5], nullptr, 10), rays, threads, reps);
+    return time_walk(mode, (uint32_t)strtoul(argv[5], nullptr, 10), rays, threads, reps, argc == 10 ? argv[9] : nullptr);
   }
   if (argc != 8) {
     fprintf(stderr, "usage: pin_traversal <blob> <rays> <mode 0|1> <ray flags> <treelet bytes> <device offset> <out>\n");

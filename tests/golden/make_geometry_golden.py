@@ -12,7 +12,7 @@ degenerate triangles, NaN and infinite ray extents, and instance matrices with
 rotation, scale and translation.
 
 Run from the repository root in a tree where the reference is available:
-    make -C oracle/ref_pin REFERENCE=/root/reference
+    make -C oracle/ref_pin REFERENCE=<reference checkout>
     python tests/golden/make_geometry_golden.py
 The committed .npz is what tests/test_golden.py checks the oracle against.
 """

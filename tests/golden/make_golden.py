@@ -4,7 +4,7 @@ reachable in each, the fields decoded by the REFERENCE's own header
 oracle/ref_pin/pin_decoders.cpp.
 
 Run from the repository root in a tree where the reference is available:
-    make -C oracle/ref_pin REFERENCE=/root/reference
+    make -C oracle/ref_pin REFERENCE=<reference checkout>
     python tests/golden/make_golden.py
 The committed .npz is what tests/test_golden.py checks the oracle against.
 """

@@ -14,7 +14,7 @@ digest of each case's result words and a SHA-256 digest of the case words,
 which the test regenerates with case_words().
 
 Run from the repository root in a tree where the reference is available:
-    make -C oracle/ref_pin REFERENCE=/root/reference
+    make -C oracle/ref_pin REFERENCE=<reference checkout>
     python tests/golden/make_prefetch_golden.py
 The committed .npz is what tests/test_golden.py checks the oracle against.
 

@@ -25,7 +25,7 @@ SHA-256 digests of the case words are kept as well; the test regenerates the
 cases with case_words() / stride_streams().
 
 Run from the repository root in a tree where the reference is available:
-    make -C oracle/ref_pin REFERENCE=/root/reference
+    make -C oracle/ref_pin REFERENCE=<reference checkout>
     python tests/golden/make_rtunit_golden.py
 The committed .npz is what tests/test_golden.py checks the oracle against.
 """

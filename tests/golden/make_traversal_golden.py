@@ -18,7 +18,7 @@ scenes) and SHA-256 digests of the blob and the rays, which the test
 regenerates with the library's seeded generators.
 
 Run from the repository root in a tree where the reference is available:
-    make -C oracle/ref_pin REFERENCE=/root/reference
+    make -C oracle/ref_pin REFERENCE=<reference checkout>
     python tests/golden/make_traversal_golden.py
 The committed .npz is what tests/test_golden.py checks the oracle against.
 """

@@ -12,7 +12,7 @@ scenes of the library's generator; the test regenerates them and checks
 their SHA-256 first.
 
 Run from the repository root in a tree where the reference is available:
-    make -C oracle/ref_pin REFERENCE=/root/reference
+    make -C oracle/ref_pin REFERENCE=<reference checkout>
     python tests/golden/make_treelet_golden.py
 The committed .npz is what tests/test_golden.py checks the oracle against.
 """

@@ -204,3 +204,49 @@ def coplanar_ray():
 
 
 COPLANAR = [(0, S), (1, I), (2, IL), (4, S), (5, I), (6, D), (6, Q)]
+
+
+# ------------------------------------------------------------- deep stacks
+# A BLAS that is a chain of `depth` internal nodes under one identity
+# instance.  Chain node k (unit 5 + 6k) has five quad leaves (units +1..+5)
+# and, except the last, the next chain node (unit +6) as its sixth child; every
+# box spans [-1,3]x[-1,3]x[0,15].  traceRay (vulkan_ray_tracing.cc:2309-3076)
+# descends the first hit internal child and pushes the other hit children, so
+# a ray that hits the boxes holds 5 (k + 1) leaves on its stack at chain node
+# k: 5 * depth at the bottom, before any leaf is popped.  Leaf j of node k has
+# its triangle in the plane z = 0.5 + 14 (5k + j) / (5 depth) and
+# PrimitiveIndex0 1000 + 5k + j.
+def deep_chain_blob(depth: int) -> np.ndarray:
+    full = ((0, 0, 0), (64, 64, 240))
+    units = [
+        _header(64, (-1, -1, 0), (3, 3, 15)),
+        _internal((-1, -1, 0), 1, (4, 4, 4), [(2, 1) + full]),
+        _instance(2 * 64, 11),
+        _header(64, (-1, -1, 0), (3, 3, 15)),
+    ]
+    n_leaves = 5 * depth
+    for k in range(depth):
+        kids = [(1, 4) + full] * 5 + ([(1, 0) + full] if k + 1 < depth else [])
+        units.append(_internal((-1, -1, 0), 1, (4, 4, 4), kids))
+        for j in range(5):
+            i = 5 * k + j
+            units.append(_quad(0.5 + 14.0 * i / n_leaves, 1000 + i))
+    blob = b"".join(units)
+    assert len(blob) == (5 + 6 * depth) * 64
+    return np.frombuffer(blob, np.uint8).copy()
+
+
+def grid_rays(n: int = 16):
+    """n x n rays from z = -5 towards +z over x, y in [-2, 4]: rays inside
+    [-1, 3]^2 hit every box (those with x + y > 2 miss every triangle), the
+    others miss the TLAS box."""
+    from treelet_rt import RAY_DTYPE
+
+    g = np.linspace(-2.0, 4.0, n, dtype=np.float32)
+    x, y = np.meshgrid(g, g)
+    r = np.zeros(n * n, RAY_DTYPE)
+    r["origin"] = np.stack([x.ravel(), y.ravel(), np.full(n * n, -5.0, np.float32)], 1)
+    r["dir"] = (0.0, 0.0, 1.0)
+    r["tmin"] = 1e-4
+    r["tmax"] = 1e30
+    return r

@@ -123,7 +123,7 @@ struct rt_scene {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
-  rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096};
+  rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096, rtk::kWaitTries};
   // host-buffer path: a copy-in stream, two trace streams (chunk c on
   // stream / stream2 by parity, so one chunk's launch fills the SMs that the
   // previous chunk's last rays leave idle), a copy-out stream, and events
@@ -319,6 +319,10 @@ rt_status merge_tuning(const rt_tuning& cur, const rt_tuning* t, rt_tuning& n) {
       return rti::fail(RT_ERR_INVALID, "pinned_bytes must be 256..229376 or RT_TUNING_OFF");
     n.pinned_bytes = t->pinned_bytes;
   }
+  if (t->wait_tries) {
+    if (t->wait_tries > (1u << 24)) return rti::fail(RT_ERR_INVALID, "wait_tries must be 1..2^24");
+    n.wait_tries = t->wait_tries;
+  }
   return RT_OK;
 }
 
@@ -329,6 +333,7 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
                      bool keep) {
   a.epoch = t.staged_epoch;
   a.refill = t.refill_lanes;
+  a.wait_tries = t.wait_tries;
   if (!keep) {
     RT_CUDA(cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, st));
     RT_CUDA(cudaMemsetAsync(a.status, 0, sizeof(uint32_t), st));
@@ -685,10 +690,29 @@ rt_status host_finish(rt_scene* s, rt_status st) {
     if (e == cudaSuccess) e = ex;
   }
   if (st == RT_OK && e != cudaSuccess) return cuda_fail(e, "rt_trace_host");
+  if (st == RT_OK) return rti::check_device_status(s, "rt_trace_host");
   return st;
 }
 
 }  // namespace
+
+namespace rti {
+
+// Reads the scene's device status word after its traces have finished and
+// turns a bounded wait that gave up into RT_ERR_TIMEOUT.  Hit records stay
+// valid then: the kernel stops staging and reads nodes from global memory.
+rt_status check_device_status(rt_scene* s, const char* who) {
+  uint32_t status = 0;
+  const cudaError_t e = cudaMemcpy(&status, s->d_status, sizeof(status), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  if (status & rtk::kStatusTimeout)
+    return fail(RT_ERR_TIMEOUT, std::string(who) +
+                                    ": a bounded staging wait gave up (hit records are valid; staging was switched "
+                                    "off for the rest of the launch)");
+  return RT_OK;
+}
+
+}  // namespace rti
 
 extern "C" {
 
@@ -1016,7 +1040,7 @@ struct rt_batch {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;
-  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, RT_TUNING_OFF};  // batches pin nothing
+  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, RT_TUNING_OFF, rtk::kWaitTries};  // batches pin nothing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };

@@ -25,6 +25,10 @@ rt_status fail(rt_status s, const std::string& msg);
 // Host-side structural check of a blob; returns false with a message.
 bool validate_blob(const uint8_t* b, uint64_t n, std::string* err);
 
+// After the scene's traces have finished: RT_ERR_TIMEOUT if a bounded device
+// wait of the last launch gave up, else RT_OK.
+rt_status check_device_status(rt_scene* s, const char* who);
+
 // rt_trace_host runs a call of 2^20 rays or more as 4 chunks of 1/8, 3/8,
 // 3/8 and 1/8 of the rays (small first and last chunks shorten the copy-in
 // before the first trace and the copy-out after the last), one of 2^19 or

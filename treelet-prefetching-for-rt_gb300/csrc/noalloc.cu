@@ -17,6 +17,12 @@
 //  * Every call on a device uses the same array.  Calls whose work overlaps
 //    on the GPU (from several host threads, or several scenes on one device)
 //    race on it; callers must serialise them.
+//  * The call runs on the calling thread's per-thread default stream, while
+//    the scene's ray hand-out counter, trace counters and status word are
+//    shared with every other trace of that scene (rt_trace, rt_trace_host,
+//    rt_trace_batch).  A call that overlaps any other trace of the same scene
+//    on the GPU races on those as well: serialise them too.
+//  * The caller's current device is restored before the call returns.
 //  * The array keeps the last call's contents.  Nothing in it needs to start
 //    at zero: each call overwrites the rays and flags it uses and the kernel
 //    writes every hit record it returns.
@@ -63,6 +69,35 @@ rt_status scratch_address(int device, unsigned char** out) {
 
 }  // namespace
 
+namespace {
+
+rt_status trace_noalloc(rt_scene* scene, int device, const rt_ray* rays, const uint32_t* flags,
+                        uint32_t default_flags, uint32_t n, uint32_t mode, rt_hit* hits) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
+  unsigned char* base = nullptr;
+  rt_status st = scratch_address(device, &base);
+  if (st != RT_OK) return st;
+  rt_ray* d_rays = reinterpret_cast<rt_ray*>(base);
+  uint32_t* d_flags = flags ? reinterpret_cast<uint32_t*>(base + kRayBytes) : nullptr;
+  rt_hit* d_hits = reinterpret_cast<rt_hit*>(base + kRayBytes + kFlagBytes);
+  cudaStream_t s = cudaStreamPerThread;
+  e = cudaMemcpyAsync(d_rays, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && flags)
+    e = cudaMemcpyAsync(d_flags, flags, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
+  st = rt_trace(scene, d_rays, d_flags, default_flags, n, mode, d_hits, nullptr, s);
+  if (st != RT_OK) return st;
+  e = cudaMemcpyAsync(hits, d_hits, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
+  // a bounded wait inside the kernel that gave up (results stay valid:
+  // staging was switched off for the rest of that launch)
+  return rti::check_device_status(scene, "rt_trace_host_noalloc");
+}
+
+}  // namespace
+
 extern "C" rt_status rt_trace_host_noalloc(rt_scene* scene, const rt_ray* rays, const uint32_t* flags,
                                            uint32_t default_flags, uint32_t n, uint32_t mode, rt_hit* hits) {
   if (!scene) return rti::fail(RT_ERR_INVALID, "rt_trace_host_noalloc: NULL scene");
@@ -80,23 +115,13 @@ extern "C" rt_status rt_trace_host_noalloc(rt_scene* scene, const rt_ray* rays, 
   cudaPointerAttributes attr{};
   cudaError_t e = cudaPointerGetAttributes(&attr, dblob);
   if (e != cudaSuccess) return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
-  e = cudaSetDevice(attr.device);
+  int caller_device = 0;
+  e = cudaGetDevice(&caller_device);
   if (e != cudaSuccess) return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
-  unsigned char* base = nullptr;
-  st = scratch_address(attr.device, &base);
-  if (st != RT_OK) return st;
-  rt_ray* d_rays = reinterpret_cast<rt_ray*>(base);
-  uint32_t* d_flags = flags ? reinterpret_cast<uint32_t*>(base + kRayBytes) : nullptr;
-  rt_hit* d_hits = reinterpret_cast<rt_hit*>(base + kRayBytes + kFlagBytes);
-  cudaStream_t s = cudaStreamPerThread;
-  e = cudaMemcpyAsync(d_rays, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && flags)
-    e = cudaMemcpyAsync(d_flags, flags, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
-  st = rt_trace(scene, d_rays, d_flags, default_flags, n, mode, d_hits, nullptr, s);
-  if (st != RT_OK) return st;
-  e = cudaMemcpyAsync(hits, d_hits, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
-  return RT_OK;
+  st = trace_noalloc(scene, attr.device, rays, flags, default_flags, n, mode, hits);
+  // the caller's current device, as it was on entry
+  e = cudaSetDevice(caller_device);
+  if (st == RT_OK && e != cudaSuccess)
+    return rti::fail(RT_ERR_CUDA, std::string("rt_trace_host_noalloc: ") + cudaGetErrorString(e));
+  return st;
 }

@@ -75,6 +75,7 @@ struct TraceArgs {
   uint32_t refill;             // idle lanes of a warp that trigger a refill
   uint32_t min_votes;          // lanes that must want a treelet before a warp stages it
   const uint32_t* hint;        // staged: predicted next treelet per (treelet, direction octant), or null
+  uint32_t wait_tries;         // staged: probes of the wait for the pinned image before staging stops
 };
 
 struct Recorder {

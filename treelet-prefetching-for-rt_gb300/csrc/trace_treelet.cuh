@@ -394,9 +394,13 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase with the given parity; false if it gave up.
+// The first of the max_tries probes does not block (test_wait), the others
+// may suspend the thread for a while each (try_wait).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_tries) {
   const uint32_t addr = smem_u32(bar);
-  for (uint32_t i = 0; i < max_tries; ++i) {
+  if (max_tries == 0) return false;
+  if (mbar_test(bar, parity)) return true;
+  for (uint32_t i = 1; i < max_tries; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -472,7 +476,7 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_sta
       for (uint32_t off = 0; off < a.pin_bytes; off += kPinChunk)
         bulk_copy_g2s(smem0 + off, reinterpret_cast<const uint8_t*>(a.pin_image) + off,
                       min(kPinChunk, a.pin_bytes - off), &pin_bar);
-      pin_ok = mbar_wait(&pin_bar, 0, kWaitTries) ? 1u : 0u;
+      pin_ok = mbar_wait(&pin_bar, 0, a.wait_tries) ? 1u : 0u;
       if (!pin_ok) atomicOr(a.status, kStatusTimeout);
     }
   }

@@ -2,6 +2,7 @@
 
     libtreelet_rt.so   <- csrc/*.cpp (g++) + csrc/capi.cu (nvcc, sm_103a)
     oracle/liboracle_rt.so  <- oracle/oracle_rt.cpp (g++), test infrastructure
+    oracle/sample_gen  <- the CPU-baseline sample writer (g++), test infrastructure
 
 Everything is compiled in place; object files go to the package's _build/
 folder.  Host code is compiled with -ffp-contract=off and device code with
@@ -25,6 +26,7 @@ INCLUDE = os.path.join(REPO, "include")
 ORACLE_DIR = os.path.join(REPO, "oracle")
 LIB_PATH = os.path.join(PKG_DIR, "libtreelet_rt.so")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle_rt.so")
+SAMPLE_GEN = os.path.join(ORACLE_DIR, "sample_gen")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
@@ -95,6 +97,18 @@ def build_oracle(verbose: bool = False, force: bool = False) -> str:
     return ORACLE_LIB
 
 
+def build_sample_gen(verbose: bool = False, force: bool = False) -> str:
+    """oracle/sample_gen: writes the CPU-baseline sample (scene blob and rays)
+    to files for the reference's walk, without loading any shared object of
+    the library (the scene and ray generators are compiled in)."""
+    srcs = [os.path.join(ORACLE_DIR, "sample_gen.cpp"), os.path.join(ORACLE_DIR, "oracle_rt.cpp"),
+            os.path.join(CSRC, "scenes.cpp"), os.path.join(CSRC, "builder.cpp")]
+    deps = srcs + [os.path.join(ORACLE_DIR, "oracle_rt.h")] + _deps()
+    if force or _stale(SAMPLE_GEN, deps):
+        _run(["g++", *HOST_FLAGS, f"-I{INCLUDE}", f"-I{CSRC}", "-o", SAMPLE_GEN, *srcs, "-lpthread"], verbose)
+    return SAMPLE_GEN
+
+
 def build_reference_pin(verbose: bool = False) -> None:
     """Builds the checker harnesses of oracle/ref_pin (the reference's own
     decoders, geometry, treelet formation and walks, compiled in place) into
@@ -111,13 +125,11 @@ def build_reference_pin(verbose: bool = False) -> None:
 
 
 def build_all(verbose: bool = False, force: bool = False) -> None:
-    with ThreadPoolExecutor(max_workers=3) as ex:
-        a = ex.submit(build_library, verbose, force)
-        b = ex.submit(build_oracle, verbose, force)
-        c = ex.submit(build_reference_pin, verbose)
-        a.result()
-        b.result()
-        c.result()
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        jobs = [ex.submit(build_library, verbose, force), ex.submit(build_oracle, verbose, force),
+                ex.submit(build_sample_gen, verbose, force), ex.submit(build_reference_pin, verbose)]
+        for j in jobs:
+            j.result()
 
 
 if __name__ == "__main__":
