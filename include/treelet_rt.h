@@ -422,12 +422,29 @@ rt_status rt_mlp_topk(rt_mlp* m, const rt_mlp_sample* samples, uint32_t n, uint3
 #define RT_PREFETCH_LATTER 3u      /* the same count from the end */
 #define RT_NO_TREELET 0xFFFFFFFFu
 
+/* Which copy of the decision runs (rt_prefetch_params.variant).  The RT unit
+ * has three: the decision block of rt_unit::cycle (shader.cc:3419-3683), the
+ * copy the pipelined treelet queue runs (-pipelined_treelet_queue,
+ * shader.cc:3780-3932: no second-prefetch rule, only the last prefetched
+ * treelet suppressed, heuristic LATTER sized at half the treelet), and the
+ * copy the treelet queue runs (-treelet_queue, shader.cc:4020-4060: the whole
+ * most popular treelet for every heuristic unless it was the last one
+ * prefetched; with no pending access it queues nothing and records "no
+ * treelet" as the last one).  RT_PREFETCH_FLUSH_ON_NEW_TREELET may be or-ed in:
+ * -flush_prefetch_queue_on_new_treelet clears the queue before a new
+ * treelet's requests (shader.cc:3579-3583, :3894-3898; the treelet queue's
+ * copy has no such step, so there it changes nothing). */
+#define RT_PREFETCH_MAIN_BLOCK 0u
+#define RT_PREFETCH_PIPELINED_QUEUE 1u
+#define RT_PREFETCH_TREELET_QUEUE 2u
+#define RT_PREFETCH_FLUSH_ON_NEW_TREELET 4u
+
 typedef struct rt_prefetch_params {
   uint32_t heuristic;       /* RT_PREFETCH_* */
   uint32_t max_queue;       /* -max_prefetch_queue_size */
   double threshold;         /* -treelet_prefetch_threshold */
   uint32_t second_prefetch; /* -prefetch_next_treelet_when_queue_empty */
-  uint32_t reserved;
+  uint32_t variant;         /* RT_PREFETCH_MAIN_BLOCK / _PIPELINED_QUEUE / _TREELET_QUEUE, | _FLUSH_ON_NEW_TREELET */
 } rt_prefetch_params;
 
 /* Per-RT-unit state carried from one decision to the next. */
@@ -449,9 +466,10 @@ typedef struct rt_prefetch_decision {
   uint32_t second_treelet; /* treelet queued by the second-prefetch rule, or RT_NO_TREELET */
 } rt_prefetch_decision;
 
-/* One decision per RT unit (shader.cc:3419-3683): n_units groups of `lanes`
- * next-access unit indices (RT_NO_TREELET = lane idle).  Device arrays;
- * state is read and updated in place.  Needs rt_treelets_form. */
+/* One decision per RT unit (shader.cc:3419-3683, or the copy params->variant
+ * names): n_units groups of `lanes` next-access unit indices (RT_NO_TREELET =
+ * lane idle).  Device arrays; state is read and updated in place.  Needs
+ * rt_treelets_form. */
 rt_status rt_prefetch_decide(rt_scene* scene, const uint32_t* next_unit, uint32_t n_units, uint32_t lanes,
                              const rt_prefetch_params* params, rt_prefetch_state* state, rt_prefetch_decision* out,
                              void* stream);
@@ -500,7 +518,8 @@ typedef struct rt_unit_config {
   uint32_t miss_latency;     /* cycles from request to data on a miss (>= 1, <= 4096) */
   uint32_t prefetcher;       /* RT_UNIT_PF_* */
   uint32_t scheduler;        /* RT_UNIT_SCHED_* (OMR / PMR need the treelet prefetcher) */
-  rt_prefetch_params decision; /* treelet prefetcher: heuristic, max queue, threshold, second prefetch */
+  rt_prefetch_params decision; /* treelet prefetcher: heuristic, max queue, threshold, second prefetch
+                                  (the main decision block: variant must be 0) */
   uint32_t prefetch_delay;   /* cycles between decisions (>= 1) */
   uint32_t load_metadata;    /* queue each member's treelet metadata before it (-load_treelet_metadata) */
   uint32_t wait_metadata;    /* strict wait for the metadata (-wait_for_metadata_load) */

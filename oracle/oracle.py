@@ -259,10 +259,12 @@ def prefetch_tally(block: np.ndarray, effectiveness: np.ndarray) -> np.ndarray:
 
 def prefetch_decide(treelets: Treelets, next_unit: np.ndarray, heuristic: int = 0, max_queue: int = 1000000,
                     threshold: float = 0.5, second_prefetch: bool = False, state: np.ndarray | None = None,
-                    queue_variant: bool = False, flush: bool = False):
+                    queue_variant: int = 0, flush: bool = False):
     """One RT unit's decision.  Returns (decision, new state) as structured
-    scalars.  queue_variant: the pipelined treelet queue's copy of the
-    decision (shader.cc:3780-3932); flush: -flush_prefetch_queue_on_new_treelet."""
+    scalars.  queue_variant: 0 the decision block of rt_unit::cycle
+    (shader.cc:3419-3683), 1 (or True) the pipelined treelet queue's copy
+    (shader.cc:3780-3932), 2 the treelet queue's copy (shader.cc:4020-4060);
+    flush: -flush_prefetch_queue_on_new_treelet."""
     nu = np.ascontiguousarray(next_unit, np.uint32)
     st = np.zeros(1, STATE_DTYPE) if state is None else np.array(state, STATE_DTYPE).reshape(1).copy()
     if state is None:

@@ -1075,9 +1075,12 @@ int oracle_trace_peaks(const uint8_t* blob, uint64_t n_bytes, const oracle_treel
 // rt_unit::cycle (shader.cc:3419-3683).  1: the copy that the pipelined
 // treelet queue runs (shader.cc:3780-3932), which has no second-prefetch rule,
 // suppresses only a repeat of the last prefetched treelet, and sizes
-// heuristic 3 at half the treelet instead of its popularity.  flush: the
+// heuristic 3 at half the treelet instead of its popularity.  2: the copy the
+// treelet queue runs (shader.cc:4020-4060): the whole most popular treelet,
+// whatever the heuristic, unless it was the last one prefetched.  flush: the
 // queue is cleared before a new treelet's chunks are queued
-// (-flush_prefetch_queue_on_new_treelet, :3579-3583 and :3894-3898).
+// (-flush_prefetch_queue_on_new_treelet, :3579-3583 and :3894-3898; the
+// treelet queue's copy has no such step).
 int oracle_prefetch_decide_ex(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
                               const rt_prefetch_params* p, rt_prefetch_state* st, rt_prefetch_decision* out,
                               uint32_t queue_variant, uint32_t flush) {
@@ -1111,6 +1114,32 @@ int oracle_prefetch_decide_ex(const oracle_treelets* tl, const uint32_t* next_un
     auto it = tl->roots.find(r);
     return it == tl->roots.end() ? nullptr : &it->second;
   };
+  if (queue_variant == 2) {  // the treelet queue's copy (shader.cc:4020-4060)
+    // no heuristic, no rejected treelet, no second prefetch, no flush: the
+    // whole most popular treelet unless it was the last one prefetched.  An
+    // empty histogram names no treelet, whose member list is empty, so the
+    // block then queues nothing but still records "no treelet" as the last
+    // prefetched one.
+    out->treelet = to_unit(prefetched_treelet_root);
+    out->count = prefetched_treelet_root ? (uint32_t)priority[prefetched_treelet_root] : 0;
+    out->total = total_threads;
+    if (last_prefetched != prefetched_treelet_root) {
+      const auto* nodes = prefetched_treelet_root ? members_of(prefetched_treelet_root) : nullptr;
+      const int n_nodes = nodes ? (int)nodes->size() : 0;
+      if ((uint64_t)n_nodes + queue <= p->max_queue) {
+        uint32_t chunks = 0;
+        for (int j = 0; j < n_nodes; ++j) chunks += ((*nodes)[j].size + 31) / 32;
+        queue += chunks;
+        out->submitted = prefetched_treelet_root ? 1 : 0;
+        out->n_members = (uint32_t)n_nodes;
+        out->chunks = chunks;
+        last_prefetched = prefetched_treelet_root;
+      }
+    }
+    st->last_prefetched = to_unit(last_prefetched);
+    st->queue_len = (uint32_t)queue;
+    return 0;
+  }
   if (p->heuristic == 0) {
     submit = true;
   } else if (prefetched_treelet_root != NONE) {

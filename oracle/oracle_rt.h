@@ -89,8 +89,10 @@ int oracle_prefetch_decide(const oracle_treelets* tl, const uint32_t* next_unit,
 /* The same with two switches: queue_variant 1 runs the copy of the decision
  * that the pipelined treelet queue uses (shader.cc:3780-3932: no second
  * prefetch, only the last prefetched treelet suppressed, heuristic 3 sized at
- * half the treelet); flush 1 clears the queue before a new treelet's chunks
- * (-flush_prefetch_queue_on_new_treelet). */
+ * half the treelet), 2 the copy the treelet queue uses (shader.cc:4020-4060:
+ * the whole most popular treelet unless it was the last prefetched one, for
+ * every heuristic); flush 1 clears the queue before a new treelet's chunks
+ * (-flush_prefetch_queue_on_new_treelet; not in the treelet queue's copy). */
 int oracle_prefetch_decide_ex(const oracle_treelets* tl, const uint32_t* next_unit, uint32_t lanes,
                               const rt_prefetch_params* p, rt_prefetch_state* state, rt_prefetch_decision* out,
                               uint32_t queue_variant, uint32_t flush);

@@ -15,7 +15,8 @@
 // Usage: pin_prefetch <blob file> <max bytes per treelet> <cases file> <out file>
 //                     [<queue variant> <flush>]
 // queue variant 1 runs the pipelined treelet queue's copy of the decision
-// (shader.cc:3780-3932, extracted into pf_decide_queue.inc) instead; flush 1
+// (shader.cc:3780-3932, extracted into pf_decide_queue.inc) instead, variant 2
+// the treelet queue's copy (shader.cc:4020-4060, pf_decide_tq.inc); flush 1
 // sets -flush_prefetch_queue_on_new_treelet.
 // cases file (uint32 words), per case: heuristic, max_queue, threshold as a
 // float's bits, second_prefetch, last_prefetched, last_prefetched_second,
@@ -67,6 +68,9 @@ class RtUnitStandIn {
   void decide_queue() {
 #include "pf_decide_queue.inc"
   }
+  void decide_treelet_queue() {
+#include "pf_decide_tq.inc"
+  }
 };
 
 int main(int argc, char** argv) {
@@ -74,7 +78,7 @@ int main(int argc, char** argv) {
     fprintf(stderr, "usage: pin_prefetch <blob> <max bytes per treelet> <cases> <out> [<queue variant> <flush>]\n");
     return 2;
   }
-  const bool queue_variant = argc == 7 && atoi(argv[5]) != 0;
+  const int queue_variant = argc == 7 ? atoi(argv[5]) : 0;
   pin::g_core.cfg.m_flush_prefetch_queue_on_new_treelet = argc == 7 && atoi(argv[6]) != 0;
   const std::vector<uint8_t> raw = read_file(argv[3]);
   if (!load_scene(argv[1], atoi(argv[2])) || raw.size() % 4) return 2;
@@ -106,7 +110,9 @@ int main(int argc, char** argv) {
         warp.threads[k % 32].RT_mem_accesses.push_back({(new_addr_type)(uintptr_t)addr_of(w[i + k])});
     }
     i += lanes;
-    if (queue_variant)
+    if (queue_variant == 2)
+      unit.decide_treelet_queue();
+    else if (queue_variant == 1)
       unit.decide_queue();
     else
       unit.decide();

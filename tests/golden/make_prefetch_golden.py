@@ -40,8 +40,10 @@ NONE = 0xFFFFFFFF
 
 # (scene, budget, cases, seed)
 SCENES = [("kat", 256, 120, 1), ("cube", 1024, 400, 2), ("shared", 512, 300, 3)]
-# (queue variant, flush) beyond the main block without flush
-VARIANTS = [(0, 1), (1, 0), (1, 1)]
+# (queue variant, flush) beyond the main block without flush: 1 is the
+# pipelined treelet queue's copy of the decision (shader.cc:3780-3932), 2 the
+# treelet queue's copy (shader.cc:4020-4060), which has no flush step
+VARIANTS = [(0, 1), (1, 0), (1, 1), (2, 0)]
 
 
 def scene(name):

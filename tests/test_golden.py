@@ -249,7 +249,7 @@ def test_prefetch_decision_matches_reference_block(built, name, budget, n_cases,
         state["last_rejected"], state["queue_len"] = c["last_rejected"], c["queue_len"]
         dec, st = orc.prefetch_decide(tl, c["next_unit"], heuristic=c["heuristic"], max_queue=c["max_queue"],
                                       threshold=c["threshold"], second_prefetch=bool(c["second"]), state=state,
-                                      queue_variant=bool(variant), flush=bool(flush))
+                                      queue_variant=int(variant), flush=bool(flush))
         queued = []
         if dec["submitted"]:
             queued += chunks(int(dec["treelet"]), int(dec["first_member"]),

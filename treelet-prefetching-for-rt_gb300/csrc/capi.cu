@@ -909,6 +909,8 @@ extern "C" rt_status rt_prefetch_decide(rt_scene* s, const uint32_t* next_unit, 
   if (lanes == 0 || lanes > (uint32_t)rtk::kMaxLanes)
     return rti::fail(RT_ERR_TOO_LARGE, "rt_prefetch_decide: lanes must be 1..1024");
   if (params->heuristic > RT_PREFETCH_LATTER) return rti::fail(RT_ERR_INVALID, "rt_prefetch_decide: unknown heuristic");
+  if ((params->variant & 3u) > RT_PREFETCH_TREELET_QUEUE || (params->variant & ~(3u | RT_PREFETCH_FLUSH_ON_NEW_TREELET)))
+    return rti::fail(RT_ERR_INVALID, "rt_prefetch_decide: unknown variant");
   if (n_units == 0) return RT_OK;
   RT_CUDA(cudaSetDevice(s->ctx->device));
   rtk::PrefetchArgs a{};
@@ -945,6 +947,7 @@ extern "C" rt_status rt_unit_replay(rt_scene* s, const rt_hit* hits, const uint3
   if (c.prefetcher > RT_UNIT_PF_STRIDE || c.scheduler > RT_UNIT_SCHED_PMR) return bad("unknown prefetcher or scheduler");
   if (c.prefetch_delay == 0) return bad("prefetch_delay must be >= 1");
   if (c.decision.heuristic > RT_PREFETCH_LATTER) return bad("unknown heuristic");
+  if (c.decision.variant != 0) return bad("the replay models the main decision block: decision.variant must be 0");
   if (n == 0) {
     RT_CUDA(cudaMemsetAsync(stats, 0, sizeof(rt_unit_stats) * c.n_rt_units, (cudaStream_t)stream));
     return RT_OK;

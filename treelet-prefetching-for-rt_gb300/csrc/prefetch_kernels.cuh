@@ -1,5 +1,6 @@
-// Treelet-prefetch decision of an RT unit (src/gpgpu-sim/shader.cc:3419-3683)
-// as a batched kernel: one CTA per RT unit.
+// Treelet-prefetch decision of an RT unit (src/gpgpu-sim/shader.cc:3419-3683,
+// or the copies the pipelined treelet queue, :3780-3932, and the treelet
+// queue, :4020-4060, run) as a batched kernel: one CTA per RT unit.
 //
 // The reference builds std::map<treelet root, count> over the first pending
 // access of every resident lane, takes the first maximum in ascending root
@@ -95,6 +96,9 @@ __global__ void __launch_bounds__(512) prefetch_decide_kernel(PrefetchArgs a) {
     nkeys = i;
   }
   rt_prefetch_state st = a.state[g];
+  const uint32_t copy = a.p.variant & 3u;
+  const bool pipelined = copy == RT_PREFETCH_PIPELINED_QUEUE;
+  const bool flush = (a.p.variant & RT_PREFETCH_FLUSH_ON_NEW_TREELET) != 0;
   rt_prefetch_decision d;
   d.treelet = best;
   d.count = best == kNone ? 0u : best_cnt;
@@ -112,6 +116,26 @@ __global__ void __launch_bounds__(512) prefetch_decide_kernel(PrefetchArgs a) {
     bd = dense_of_root(a, best);
     if (bd != kNone) n_nodes = (int)(a.member_first[bd + 1] - a.member_first[bd]);
   }
+  uint64_t queue = st.queue_len;
+  if (copy == RT_PREFETCH_TREELET_QUEUE) {
+    // the treelet queue's copy: the whole treelet whatever the heuristic,
+    // unless it was the last one prefetched; an empty histogram names no
+    // treelet (an empty member list) and is recorded as the last one
+    if (st.last_prefetched != best && (uint64_t)n_nodes + queue <= a.p.max_queue) {
+      uint32_t chunks = 0;
+      if (bd != kNone)
+        for (int j = 0; j < n_nodes; ++j) chunks += (a.member_bytes[a.member_first[bd] + j] + 31u) / 32u;
+      queue += chunks;
+      d.submitted = best != kNone ? 1u : 0u;
+      d.n_members = (uint32_t)n_nodes;
+      d.chunks = chunks;
+      st.last_prefetched = best;
+    }
+    st.queue_len = (uint32_t)queue;
+    a.state[g] = st;
+    a.out[g] = d;
+    return;
+  }
   if (a.p.heuristic == RT_PREFETCH_ALWAYS) {
     submit = true;
   } else if (best != kNone) {
@@ -124,16 +148,18 @@ __global__ void __launch_bounds__(512) prefetch_decide_kernel(PrefetchArgs a) {
         if (st.last_rejected != best) st.last_rejected = best;
       }
     } else {
-      num_nodes = (int)(((double)n_nodes * pct) + 0.5);
+      // the pipelined queue's copy sizes LATTER at half the treelet
+      const double share = (pipelined && a.p.heuristic == RT_PREFETCH_LATTER) ? 0.5 : pct;
+      num_nodes = (int)(((double)n_nodes * share) + 0.5);
       submit = true;
     }
   }
-  uint64_t queue = st.queue_len;
   if (submit && best != kNone && bd != kNone) {
-    if (st.last_prefetched != best && st.last_prefetched_second != best) {
+    if (st.last_prefetched != best && (pipelined || st.last_prefetched_second != best)) {
       const bool partial = a.p.heuristic == RT_PREFETCH_PARTIAL || a.p.heuristic == RT_PREFETCH_LATTER;
       const int num = partial ? num_nodes : n_nodes;
       if ((uint64_t)num + queue <= a.p.max_queue) {
+        if (flush) queue = 0;
         const int j0 = a.p.heuristic == RT_PREFETCH_LATTER ? n_nodes - num : 0;
         const int j1 = a.p.heuristic == RT_PREFETCH_LATTER ? n_nodes : num;
         uint32_t chunks = 0;
@@ -147,7 +173,8 @@ __global__ void __launch_bounds__(512) prefetch_decide_kernel(PrefetchArgs a) {
       }
     }
   }
-  if (a.p.second_prefetch && queue == 0 && total > 0 && distinct > 1 && st.last_prefetched == best && best != kNone) {
+  if (a.p.second_prefetch && !pipelined && queue == 0 && total > 0 && distinct > 1 && st.last_prefetched == best &&
+      best != kNone) {
     // next most popular treelet other than the last prefetched one
     uint32_t second = kNone, scnt = 0;
     uint32_t i = 0;

@@ -13,6 +13,7 @@ import ctypes as C
 import numpy as np
 
 from ._ffi import (HIT_DTYPE, MODE_PLAIN, MODE_STAGED, MODE_TREELET, NO_TREELET, PREFETCH_DECISION_DTYPE,
+                   PREFETCH_FLUSH_ON_NEW_TREELET, PREFETCH_MAIN_BLOCK, PREFETCH_PIPELINED_QUEUE, PREFETCH_TREELET_QUEUE,
                    PREFETCH_STATE_DTYPE, RAY_BAD_NODE, RAY_DTYPE, RAY_FLAG_NO_OPAQUE, RAY_FLAG_OPAQUE,
                    RAY_FLAG_SKIP_CLOSEST_HIT, RAY_FLAG_TERMINATE_ON_FIRST_HIT, RAY_HIT_PROCEDURAL,
                    RAY_STACK_OVERFLOW, RAY_TRACE_OVERFLOW, SCENE_BLOBS, SCENE_CUBE, SCENE_CUBE_PLANE,
@@ -28,6 +29,7 @@ __all__ = [
     "SCENE_TERRAIN_INSTANCES", "SCENE_BLOBS", "SCENE_CUBE", "SCENE_SHARED_BLAS", "TX_NAMES", "TX_BYTES",
     "NO_TREELET", "RAY_TRACE_OVERFLOW", "RAY_STACK_OVERFLOW", "RAY_HIT_PROCEDURAL", "RAY_BAD_NODE",
     "PREFETCH_STATE_DTYPE", "PREFETCH_DECISION_DTYPE", "PrefetchParams", "unpack_visits", "TUNING_OFF",
+    "PREFETCH_MAIN_BLOCK", "PREFETCH_PIPELINED_QUEUE", "PREFETCH_TREELET_QUEUE", "PREFETCH_FLUSH_ON_NEW_TREELET",
 ]
 
 

@@ -71,7 +71,10 @@ class TraceStats(C.Structure):
 
 class PrefetchParams(C.Structure):
     _fields_ = [("heuristic", C.c_uint32), ("max_queue", C.c_uint32), ("threshold", C.c_double),
-                ("second_prefetch", C.c_uint32), ("reserved", C.c_uint32)]
+                ("second_prefetch", C.c_uint32), ("variant", C.c_uint32)]
+
+
+PREFETCH_MAIN_BLOCK, PREFETCH_PIPELINED_QUEUE, PREFETCH_TREELET_QUEUE, PREFETCH_FLUSH_ON_NEW_TREELET = 0, 1, 2, 4
 
 
 UNIT_PF_NONE, UNIT_PF_TREELET, UNIT_PF_STRIDE = 0, 1, 2
