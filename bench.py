@@ -698,6 +698,62 @@ def run_batch(args) -> None:
     batch.close()
 
 
+def run_queues(args) -> None:
+    """The treelet-queued staged walk on the terrain workload: queue_rounds
+    swept (RT_TUNING_OFF = the staged walk without queues), primary and
+    bounce batches timed separately, with the share of node reads served from
+    shared memory and the treelet stagings per launch; hits compared with the
+    treelet-order walk's."""
+    import torch
+
+    import treelet_rt as rt
+
+    rt.lib()
+    blob, prim, _ = make_workload()
+    ctx = rt.Context(0)
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(BUDGET)
+    n = len(prim)
+    dp = torch.from_numpy(prim.view(np.uint8)).cuda()
+    hp = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+    db = torch.empty(n * 32, dtype=torch.uint8, device="cuda")
+    scene.trace(dp, hp, rt.MODE_PLAIN, n=n)
+    scene.bounce(dp, hp, db, seed=SEED + 100, n=n)
+    torch.cuda.synchronize()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    table = {}
+    for batch, d in (("primary", dp), ("bounce", db)):
+        ref = torch.empty(n * 64, dtype=torch.uint8, device="cuda")
+        scene.trace(d, ref, rt.MODE_TREELET, n=n)
+        row = {}
+        for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET)):
+            apply_tuning(scene, name, batch)
+            row[name] = round(n / _time_launch(lambda: scene.trace(d, hp, mode, stream=sp, n=n), max(3, args.steps),
+                                               flush, stream) / 1e3, 3)
+        apply_tuning(scene, "staged", batch)
+        for rounds in (rt.TUNING_OFF, 1, 2, 4, 8):
+            scene.set_tuning(queue_rounds=rounds)
+            ms = _time_launch(lambda: scene.trace(d, hp, rt.MODE_STAGED, stream=sp, n=n), max(3, args.steps), flush,
+                              stream)
+            st = scene.stats()
+            key = "staged" if rounds == rt.TUNING_OFF else f"staged_queues_{rounds}"
+            row[key] = {"mrays_s": round(n / ms / 1e3, 3), "hits_equal_treelet_order": bool(torch.equal(hp, ref)),
+                        "smem_read_fraction": round(st["smem_reads"] / max(1, st["smem_reads"] + st["gmem_reads"]), 4),
+                        "stagings": st["stagings"], "staged_bytes": st["staged_bytes"]}
+        scene.set_tuning(queue_rounds=rt.TUNING_OFF)
+        table[batch] = row
+    line = {"metric": "Mrays/s, treelet-queued staged walk vs the walks without queues", "unit": "Mrays/s",
+            "value": max(v["mrays_s"] for k, v in table["bounce"].items() if k.startswith("staged_queues")),
+            "higher_is_better": True, "n_gpus": 1,
+            "config": {"workload": WORKLOAD, "l2": "flushed", "rounds": "binned rounds of treelet queues, then the "
+                       "rays left walk to their ends"},
+            "batches": table, "dtype": "f32", "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+    scene.close()
+
+
 def run_learned(args) -> None:
     """The learned prefetcher on a 262,144-triangle unit-cube scene (a
     config-3 scene): trained on the treelet transitions of 8 jitter seeds of
@@ -896,9 +952,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="small: the same scene with 512x512x1 primary rays + bounces (profiling case)")
-    ap.add_argument("--workload", default="terrain", choices=["terrain", "ao", "batch", "learned", "replay"],
+    ap.add_argument("--workload", default="terrain", choices=["terrain", "ao", "batch", "learned", "replay", "queues"],
                     help="terrain: the headline line; ao: AO budget sweep; batch: many scenes in one launch; "
-                         "learned: the learned prefetcher against the heuristic; replay: RT-unit trace replay")
+                         "learned: the learned prefetcher against the heuristic; replay: RT-unit trace replay; "
+                         "queues: the treelet-queued staged walk, rounds swept")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--replay-rays", type=int, default=16384)
@@ -913,6 +970,8 @@ def main():
         return run_ao(args)
     if args.workload == "batch" and args.impl != "reference":
         return run_batch(args)
+    if args.workload == "queues" and args.impl != "reference":
+        return run_queues(args)
     if args.size == "small":
         global WIDTH, HEIGHT, SPP, WORKLOAD
         WIDTH = HEIGHT = 512

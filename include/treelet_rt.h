@@ -302,6 +302,13 @@ typedef struct rt_tuning {
   uint32_t wait_tries;        /* probes of a CTA's wait for its pinned treelets before it stops staging
                                  (1..2^24; the first probe does not block); the wait for copies still in
                                  flight when a CTA exits always keeps the default limit (2^22) */
+  uint32_t queue_rounds;      /* RT_MODE_STAGED: rounds of treelet queues (1..64; RT_TUNING_OFF: none, the
+                                 walk with pinned treelets and warp slots).  With queues, rays wait in
+                                 per-treelet queues between treelets; each round a warp stages one
+                                 treelet into shared memory and runs the stints of the rays queued on
+                                 it; after the last round the rays left finish without queues.  The
+                                 scene keeps the queues' device memory (about 64 + 8 * stack_depth + 16
+                                 bytes per ray) from the first such launch on. */
 } rt_tuning;
 rt_status rt_scene_set_tuning(rt_scene* scene, const rt_tuning* t);
 rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);

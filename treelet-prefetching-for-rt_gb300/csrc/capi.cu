@@ -13,6 +13,7 @@
 #include "trace_kernels.cuh"
 #include "prefetch_kernels.cuh"
 #include "replay_kernel.cuh"
+#include "trace_queued.cuh"
 #include "trace_treelet.cuh"
 #include "treelets.h"
 
@@ -90,6 +91,18 @@ bool validate_blob(const uint8_t* b, uint64_t n, std::string* err) {
   return true;
 }
 
+// Device memory of the treelet queues (trace_queued.cuh), kept by a scene
+// from its first queued launch on and grown as launches need.
+struct QueueScratch {
+  uint8_t* base = nullptr;
+  size_t bytes = 0;
+  uint4* state = nullptr;              // 64 B per ray
+  unsigned long long* slab = nullptr;  // stack_depth entries per ray
+  uint32_t *in_ray = nullptr, *in_key = nullptr, *out_ray = nullptr, *out_key = nullptr;
+  uint32_t *hist = nullptr, *offset = nullptr, *block_sum = nullptr;
+  uint32_t* ctr = nullptr;  // per round: hand-out counter, rays left
+};
+
 }  // namespace rti
 
 struct rt_scene {
@@ -123,7 +136,7 @@ struct rt_scene {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
-  rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096, rtk::kWaitTries};
+  rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096, rtk::kWaitTries, RT_TUNING_OFF};
   // host-buffer path: a copy-in stream, two trace streams (chunk c on
   // stream / stream2 by parity, so one chunk's launch fills the SMs that the
   // previous chunk's last rays leave idle), a copy-out stream, and events
@@ -131,6 +144,7 @@ struct rt_scene {
   cudaEvent_t ev_in[rti::kHostChunks] = {}, ev_done[rti::kHostChunks] = {};
   void* d_io = nullptr;
   size_t io_bytes = 0;
+  rti::QueueScratch qs;  // treelet queues of RT_MODE_STAGED with queue_rounds
 };
 
 namespace {
@@ -323,6 +337,75 @@ rt_status merge_tuning(const rt_tuning& cur, const rt_tuning* t, rt_tuning& n) {
     if (t->wait_tries > (1u << 24)) return rti::fail(RT_ERR_INVALID, "wait_tries must be 1..2^24");
     n.wait_tries = t->wait_tries;
   }
+  if (t->queue_rounds) {
+    if (t->queue_rounds != RT_TUNING_OFF && t->queue_rounds > rti::kMaxQueueRounds)
+      return rti::fail(RT_ERR_INVALID, "queue_rounds must be 1..64 or RT_TUNING_OFF");
+    n.queue_rounds = t->queue_rounds;
+  }
+  return RT_OK;
+}
+
+// The treelet-queued staged walk (trace_queued.cuh): round 0 over every ray,
+// then per round the counting sort of the rays left by the treelet they need
+// next (scan, top-level scan, scatter) and a binned round, then the last
+// round without queues.  Every kernel is stream-ordered on `st`; the scratch
+// must hold a.n rays, CAP stack entries per ray and n_bins bins.
+template <int CAP>
+rt_status launch_queued(rtk::TraceArgs& a, const rt_tuning& t, uint32_t largest_image, const rti::QueueScratch& qs,
+                        cudaStream_t st) {
+  const uint32_t rounds = t.queue_rounds;
+  const uint32_t n_bins = a.n_treelets + 1;
+  const uint32_t n_blocks = (n_bins + rtk::kBinScanItems - 1) / rtk::kBinScanItems;
+  if (n_blocks > rtk::kBinScanItems)
+    return rti::fail(RT_ERR_TOO_LARGE, "treelet queues: more than 2^24 treelets");
+  RT_CUDA(cudaMemsetAsync(qs.ctr, 0, sizeof(uint32_t) * 2 * (rti::kMaxQueueRounds + 1), st));
+  RT_CUDA(cudaMemsetAsync(qs.hist, 0, sizeof(uint32_t) * n_bins, st));
+  const uint32_t bt = rtk::kStagedMaxThreads;
+  // a warp's slot holds a whole treelet of the 8 KiB budgets, the first
+  // 8 KiB of larger ones (three CTAs of eight warps per SM); the rest of a
+  // larger treelet is read from global memory
+  const uint32_t slot = std::min((largest_image + 127u) & ~127u, rtk::kQueueSlotMax);
+  const size_t dyn = (size_t)(bt / 32) * slot + 128;
+  auto kern = rtk::trace_queued_kernel<CAP, false>;
+  auto fin = rtk::trace_queued_kernel<CAP, true>;
+  RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  RT_CUDA(cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, 128));
+  const uint32_t grid = persistent_grid((const void*)kern, bt, a.n, dyn);
+  const uint32_t grid_fin = persistent_grid((const void*)fin, bt, a.n, 128);
+  a.min_votes = t.staged_min_votes;
+  rtk::QueueArgs q{};
+  q.state = qs.state;
+  q.slab = qs.slab;
+  q.hist = qs.hist;
+  q.n_bins = n_bins;
+  q.slot_bytes = slot;
+  for (uint32_t k = 0; k < rounds; ++k) {
+    if (k > 0) {
+      // the rays left after round k-1, grouped by the treelet they need
+      rtk::bin_scan_kernel<<<n_blocks, 1024, 0, st>>>(qs.hist, qs.offset, qs.block_sum, n_bins);
+      rtk::bin_scan_top_kernel<<<1, 1024, 0, st>>>(qs.block_sum, n_blocks);
+      rtk::bin_scatter_kernel<<<std::min<uint32_t>((a.n + 255) / 256, 4096), 256, 0, st>>>(
+          qs.out_ray, qs.out_key, qs.ctr + 2 * (k - 1) + 1, qs.offset, qs.block_sum, qs.in_ray, qs.in_key);
+    }
+    q.in_ray = k ? qs.in_ray : nullptr;
+    q.in_key = k ? qs.in_key : nullptr;
+    q.n_in = k ? qs.ctr + 2 * (k - 1) + 1 : nullptr;
+    q.take = qs.ctr + 2 * k;
+    q.out_ray = qs.out_ray;
+    q.out_key = qs.out_key;
+    q.n_out = qs.ctr + 2 * k + 1;
+    kern<<<grid, bt, dyn, st>>>(a, q);
+  }
+  // the rays left walk to their ends; the queue lists of the last round are
+  // its input as they are (no sort)
+  q.in_ray = qs.out_ray;
+  q.in_key = qs.out_key;
+  q.n_in = qs.ctr + 2 * (rounds - 1) + 1;
+  q.take = qs.ctr + 2 * rounds;
+  q.out_ray = q.out_key = q.n_out = nullptr;
+  q.slot_bytes = 0;
+  fin<<<grid_fin, bt, 128, st>>>(a, q);
+  RT_CUDA(cudaGetLastError());
   return RT_OK;
 }
 
@@ -330,7 +413,7 @@ rt_status merge_tuning(const rt_tuning& cur, const rt_tuning* t, rt_tuning& n) {
 // one call add up), then launches the kernel of `mode` with stack depth CAP.
 template <int CAP>
 rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint32_t largest_image, cudaStream_t st,
-                     bool keep) {
+                     bool keep, const rti::QueueScratch* qs) {
   a.epoch = t.staged_epoch;
   a.refill = t.refill_lanes;
   a.wait_tries = t.wait_tries;
@@ -347,6 +430,9 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
     const uint32_t bt = t.block_threads;
     auto kern = a.n_items ? rtk::trace_treelet_kernel<CAP, true> : rtk::trace_treelet_kernel<CAP, false>;
     kern<<<persistent_grid((const void*)kern, bt, a.n), bt, 0, st>>>(a);
+  } else if (qs) {
+    if (a.n_items) return rti::fail(RT_ERR_INVALID, "staged traces run over one scene");
+    return launch_queued<CAP>(a, t, largest_image, *qs, st);
   } else {
     // the staged kernel is compiled for launches over one scene
     if (a.n_items) return rti::fail(RT_ERR_INVALID, "staged traces run over one scene");
@@ -378,15 +464,57 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
 // Stack depths compiled in (entries per stack per ray); a ray that needs more
 // is flagged RT_RAY_STACK_OVERFLOW.
 rt_status launch_trace(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint32_t largest_image,
-                       cudaStream_t st, bool keep = false) {
+                       cudaStream_t st, bool keep = false, const rti::QueueScratch* qs = nullptr) {
   switch (t.stack_depth) {
     case 48:
-      return launch_cap<48>(a, mode, t, largest_image, st, keep);
+      return launch_cap<48>(a, mode, t, largest_image, st, keep, qs);
     case 160:
-      return launch_cap<160>(a, mode, t, largest_image, st, keep);
+      return launch_cap<160>(a, mode, t, largest_image, st, keep, qs);
     default:
-      return launch_cap<96>(a, mode, t, largest_image, st, keep);
+      return launch_cap<96>(a, mode, t, largest_image, st, keep, qs);
   }
+}
+
+// True when a staged launch of the scene runs with treelet queues.
+bool queued(const rt_scene* s, uint32_t mode) {
+  return mode == RT_MODE_STAGED && s->tuning.queue_rounds != RT_TUNING_OFF && s->tuning.queue_rounds > 0;
+}
+
+// Grows the scene's queue memory to n rays (stack_depth entries per ray).
+rt_status ensure_queue_scratch(rt_scene* s, uint32_t n) {
+  rti::QueueScratch& q = s->qs;
+  const uint64_t cap = s->tuning.stack_depth;
+  const uint64_t n_bins = (uint64_t)s->part.roots.size() + 1;
+  const uint64_t n_blocks = (n_bins + rtk::kBinScanItems - 1) / rtk::kBinScanItems;
+  auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
+  const uint64_t b_state = al(64ull * n), b_slab = al(8ull * cap * n), b_list = al(4ull * n);
+  const uint64_t b_bins = al(4ull * n_bins), b_blocks = al(4ull * n_blocks);
+  const uint64_t b_ctr = al(sizeof(uint32_t) * 2 * (rti::kMaxQueueRounds + 1));
+  const uint64_t need = b_state + b_slab + 4 * b_list + 2 * b_bins + b_blocks + b_ctr;
+  if (need > q.bytes) {
+    cudaFree(q.base);
+    q = rti::QueueScratch{};
+    rt_status st = dalloc(&q.base, need);
+    if (st != RT_OK) return st;
+    q.bytes = need;
+  }
+  uint8_t* p = q.base;
+  auto take = [&](uint64_t b) {
+    uint8_t* r = p;
+    p += b;
+    return r;
+  };
+  q.state = reinterpret_cast<uint4*>(take(b_state));
+  q.slab = reinterpret_cast<unsigned long long*>(take(b_slab));
+  q.in_ray = reinterpret_cast<uint32_t*>(take(b_list));
+  q.in_key = reinterpret_cast<uint32_t*>(take(b_list));
+  q.out_ray = reinterpret_cast<uint32_t*>(take(b_list));
+  q.out_key = reinterpret_cast<uint32_t*>(take(b_list));
+  q.hist = reinterpret_cast<uint32_t*>(take(b_bins));
+  q.offset = reinterpret_cast<uint32_t*>(take(b_bins));
+  q.block_sum = reinterpret_cast<uint32_t*>(take(b_blocks));
+  q.ctr = reinterpret_cast<uint32_t*>(take(b_ctr));
+  return RT_OK;
 }
 
 }  // namespace
@@ -469,6 +597,7 @@ rt_status rt_scene_destroy(rt_scene* s) {
   cudaFree(s->d_status);
   cudaFree(s->d_queue);
   cudaFree(s->d_io);
+  cudaFree(s->qs.base);
   for (uint32_t c = 0; c < rti::kHostChunks; ++c) {
     if (s->ev_in[c]) cudaEventDestroy(s->ev_in[c]);
     if (s->ev_done[c]) cudaEventDestroy(s->ev_done[c]);
@@ -665,6 +794,11 @@ rt_status trace_launch(rt_scene* s, const rt_ray* rays, const uint32_t* flags, u
   a.status = s->d_status;
   a.queue = queue;
   a.hint = s->d_hint;
+  if (queued(s, mode)) {
+    rt_status qst = ensure_queue_scratch(s, n);
+    if (qst != RT_OK) return qst;
+    return launch_trace(a, mode, s->tuning, s->slot_bytes, st, keep, &s->qs);
+  }
   return launch_trace(a, mode, s->tuning, s->slot_bytes, st, keep);
 }
 
@@ -825,7 +959,11 @@ rt_status rt_trace_host(rt_scene* s, const rt_ray* rays, const uint32_t* flags, 
   // Chunks pipeline the copies with the traces: rays of chunk c+1 go in and
   // hits of chunk c-1 come out while chunk c is traced.
   uint64_t bound[rti::kHostChunks + 1];
-  const uint32_t chunks = rti::host_chunk_bounds(n, bound);
+  // a queued staged launch runs whole: its queues are the scene's, one set
+  uint32_t chunks = 1;
+  bound[0] = 0;
+  bound[1] = n;
+  if (!queued(s, mode)) chunks = rti::host_chunk_bounds(n, bound);
   // counters of the whole call start at zero, ahead of every chunk's copy-in
   RT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, s->xin));
   RT_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->xin));
@@ -1043,7 +1181,7 @@ struct rt_batch {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;
-  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, RT_TUNING_OFF, rtk::kWaitTries};  // batches pin nothing
+  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, RT_TUNING_OFF, rtk::kWaitTries, RT_TUNING_OFF};  // batches pin nothing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };

@@ -35,6 +35,8 @@ rt_status check_device_status(rt_scene* s, const char* who);
 // more as 2 halves, and smaller calls whole.  Each chunk costs about one
 // launch's tail (tens of microseconds on a full GPU), so more chunks lose.
 constexpr uint32_t kHostChunks = 4;
+// Rounds of treelet queues a staged launch may run (rt_tuning.queue_rounds).
+constexpr uint32_t kMaxQueueRounds = 64;
 inline uint32_t host_chunk_bounds(uint32_t n, uint64_t* lo) {
   const uint32_t chunks = n >= (1u << 20) ? 4u : n >= (1u << 19) ? 2u : 1u;
   static const uint32_t kEighths[3][5] = {{0, 8}, {0, 4, 8}, {0, 1, 4, 7, 8}};

@@ -36,14 +36,21 @@ constexpr uint32_t kRouteOther = 6, kRouteInst = 12;  // route bits (treelets.h)
 // with the world ray in registers at three CTAs per SM.
 constexpr int kColdWords = 9;
 
-template <int CAP, bool STAGED, bool MULTI>
+// SLAB = true keeps the other-treelet stack in a per-ray slab of global
+// memory (`ot`, CAP entries) instead of the local array, so that a ray can
+// stop between treelets and go on later in another thread: the treelet-queued
+// walk (trace_queued.cuh).  The local array then holds only the current
+// stack and the cold tail.
+template <int CAP, bool STAGED, bool MULTI, bool SLAB = false>
 struct Walker {
   static constexpr bool kColdWorld = !STAGED;
+  static constexpr int kOtLocal = SLAB ? 0 : CAP;  // other-stack entries in the local array
   rtm::V3 O, idir;  // world ray (registers only when !kColdWorld)
   float tmin, tmax, min_thit;
   bool terminate, fast, ic_fast;  // FAST min/max allowed for the world / object ray
   uint32_t status;
-  unsigned long long* stk;  // 2 * CAP + kColdWords entries, a local array of the kernel
+  unsigned long long* stk;  // CAP + kOtLocal + kColdWords entries, a local array of the kernel
+  unsigned long long* ot;   // SLAB: the ray's other-treelet stack in global memory
   int ncu, not_;            // entries on cu and on ot
   // The top of `cu` when it was pushed by the previous node visit: the node
   // the walk pops next, kept in a register instead of a local-memory round
@@ -66,8 +73,10 @@ struct Walker {
     ncu = not_ = 0;
   }
 
-  // ---- the cold tail: stk[2 CAP + k]
-  __device__ __forceinline__ unsigned long long& cold(int k) const { return stk[2 * CAP + k]; }
+  // ---- the cold tail: stk[CAP + kOtLocal + k]
+  __device__ __forceinline__ unsigned long long& cold(int k) const { return stk[CAP + kOtLocal + k]; }
+  // ---- entry i of the other-treelet stack
+  __device__ __forceinline__ unsigned long long& ot_at(int i) const { return SLAB ? ot[i] : stk[CAP + i]; }
   static __device__ __forceinline__ unsigned long long pack(float a, float b) {
     return (unsigned long long)__float_as_uint(a) | ((unsigned long long)__float_as_uint(b) << 32);
   }
@@ -123,7 +132,7 @@ struct Walker {
     unsigned long long e;
     if (nxt) e = nxt;
     else if (ncu > 0) e = stk[ncu - 1];
-    else if (not_ > 0) e = stk[CAP + not_ - 1];
+    else if (not_ > 0) e = ot_at(not_ - 1);
     else return kNone;
     if ((uint32_t)e & kEPin) return kNone;
     const uint32_t unit = (uint32_t)e >> kEShift;
@@ -138,7 +147,10 @@ struct Walker {
     const bool store = !same || nxt != 0;
     const int cnt = same ? ncu : not_;
     const bool ok = cnt < CAP;
-    if (store && ok) stk[same ? cnt : CAP + cnt] = same ? nxt : e;
+    if (store && ok) {
+      if (SLAB) *(same ? stk + cnt : ot + cnt) = same ? nxt : e;
+      else stk[same ? cnt : CAP + cnt] = same ? nxt : e;
+    }
     if (store && !ok) status |= RT_RAY_STACK_OVERFLOW;
     ncu += (same && store && ok) ? 1 : 0;
     not_ += (!same && ok) ? 1 : 0;
@@ -185,6 +197,55 @@ struct Walker {
     }
   }
 
+  // ---- the treelet-queued walk (SLAB): a ray's state between two treelets,
+  // 64 bytes: the ray (origin, tmin, direction, tmax), then min_thit, status
+  // (bit 31: terminate on first hit), transactions and bytes recorded, the
+  // closest leaf, its instance, its object-space t, and the other-treelet
+  // stack's size.  The current-treelet stack is empty between treelets.
+  static constexpr uint32_t kTerminateBit = 0x80000000u;
+
+  __device__ __forceinline__ void save_ray(uint4* st) const {
+    const rtm::V3 o = world_o(), d = dir();
+    st[0] = make_uint4(__float_as_uint(o.x), __float_as_uint(o.y), __float_as_uint(o.z), __float_as_uint(tmin));
+    st[1] = make_uint4(__float_as_uint(d.x), __float_as_uint(d.y), __float_as_uint(d.z), __float_as_uint(tmax));
+  }
+
+  __device__ __forceinline__ void suspend(uint4* st) const {
+    const unsigned long long h = cold(2);
+    st[2] = make_uint4(__float_as_uint(min_thit), status | (terminate ? kTerminateBit : 0u), rec.n, rec.bytes);
+    st[3] = make_uint4((uint32_t)h, (uint32_t)(h >> 32), (uint32_t)cold(3), (uint32_t)not_);
+  }
+
+  __device__ __forceinline__ void resume(const TraceArgs& a, uint32_t r, const uint4* st) {
+    v = scene_of<MULTI>(a, r);
+    const uint4 q0 = st[0], q1 = st[1], q2 = st[2], q3 = st[3];
+    const rtm::V3 o = rtm::v3(__uint_as_float(q0.x), __uint_as_float(q0.y), __uint_as_float(q0.z));
+    const rtm::V3 D = rtm::v3(__uint_as_float(q1.x), __uint_as_float(q1.y), __uint_as_float(q1.z));
+    tmin = __uint_as_float(q0.w);
+    tmax = __uint_as_float(q1.w);
+    min_thit = __uint_as_float(q2.x);
+    status = q2.y & ~kTerminateBit;
+    terminate = (q2.y & kTerminateBit) != 0;
+    rec = Counts{a.cap, q2.z, q2.w};
+    cold(2) = (unsigned long long)q3.x | ((unsigned long long)q3.y << 32);
+    cold(3) = (unsigned long long)q3.z;
+    cold(4) = reinterpret_cast<unsigned long long>(a.visits ? a.visits + (uint64_t)r * a.cap : nullptr);
+    cold(5) = reinterpret_cast<unsigned long long>(a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr);
+    nxt = 0;
+    ncu = 0;
+    not_ = (int)q3.w;
+    set_dir(D);
+    ic.unit = kNone;
+    ic_fast = false;
+    smem_reads = gmem_reads = 0;
+    set_world(o, rtm::calculate_idir(D));
+    fast = rtd::finite_ray(o, D, tmin, tmax);
+  }
+
+  // True while the walk is inside its current treelet: the next pop would
+  // come from the current-treelet stack.
+  __device__ __forceinline__ bool in_treelet() const { return nxt != 0 || ncu > 0; }
+
   // Visits one node; `lookup(unit, meta)` returns the shared-memory address
   // of a node staged in a warp slot, else 0.
   template <class Lookup>
@@ -192,7 +253,7 @@ struct Walker {
     const bool from_cu = nxt != 0 || ncu > 0;  // :1748-1754
     unsigned long long e = nxt;
     if (!nxt) {
-      e = stk[from_cu ? ncu - 1 : CAP + not_ - 1];
+      e = SLAB ? (from_cu ? stk[ncu - 1] : ot[not_ - 1]) : stk[from_cu ? ncu - 1 : CAP + not_ - 1];
       ncu -= from_cu ? 1 : 0;
       not_ -= from_cu ? 0 : 1;
     }

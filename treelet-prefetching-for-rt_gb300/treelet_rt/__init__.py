@@ -262,10 +262,11 @@ class Scene:
         check(lib().rt_scene_set_stage_hints(self._h, h.ctypes.data))
 
     def set_tuning(self, block_threads=0, staged_threads=0, staged_epoch=0, staged_slots=0, refill_lanes=0,
-                   staged_slot_bytes=0, staged_min_votes=0, stack_depth=0, pinned_bytes=0, wait_tries=0) -> None:
-        """0 keeps a value; TUNING_OFF switches staged_slots / pinned_bytes off."""
+                   staged_slot_bytes=0, staged_min_votes=0, stack_depth=0, pinned_bytes=0, wait_tries=0,
+                   queue_rounds=0) -> None:
+        """0 keeps a value; TUNING_OFF switches staged_slots / pinned_bytes / queue_rounds off."""
         t = Tuning(block_threads, staged_threads, staged_epoch, staged_slots, refill_lanes, staged_slot_bytes,
-                   staged_min_votes, stack_depth, pinned_bytes, wait_tries)
+                   staged_min_votes, stack_depth, pinned_bytes, wait_tries, queue_rounds)
         check(lib().rt_scene_set_tuning(self._h, C.byref(t)))
 
     def set_pin_order(self, order=None) -> None:
