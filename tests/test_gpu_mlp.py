@@ -61,6 +61,11 @@ def test_training_and_gain_over_heuristic(ctx):
     print(f"\nheld-out next-treelet hit rate (top-1, top-4): heuristic {h_pop}, mlp {h_mlp}, mlp+fallback {h_mix}")
     # the network learned the transitions far above chance (1 / n_treelets)
     assert h_mlp[1] > 0.3
+    # and predicts held-out transitions better than the popularity heuristic
+    # without it: the ray's origin and direction tell it which child treelet
+    # comes next, which the per-treelet counts cannot
+    assert h_mlp[1] > h_pop[1] + 0.01, (h_mlp, h_pop)
+    assert h_mix[1] > h_pop[1], (h_mix, h_pop)
     # hints from the network stage treelets without changing any result
     hints = L.hint_table(mlp, train, n_tl)
     rays = rt.camera_rays(cam, 128, 128, 1, 9, 1e-4, 1e30)

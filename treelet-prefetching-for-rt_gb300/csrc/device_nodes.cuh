@@ -110,6 +110,47 @@ __device__ __forceinline__ bool slab_hit(float lx, float ly, float lz, float hx,
   return h;
 }
 
+// Two-wide FP32 arithmetic (add / sub / mul / fma .rn.f32x2, sm_100 and
+// later): one instruction computes two lanes, each rounded exactly as the
+// scalar instruction rounds it (IEEE round to nearest even, subnormals
+// kept), so the results are bit for bit those of two scalar operations.  The
+// slab test pairs a child's x and y planes in them.
+__device__ __forceinline__ unsigned long long f2_pack(float x, float y) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_pack_bits(uint32_t x, uint32_t y) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(x), "r"(y));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long r, float& x, float& y) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// Bits of byte b of the node placed in the mantissa of 2^23 (byte_as_float
+// before its subtraction of 2^23).
+__device__ __forceinline__ uint32_t byte_bits(const Node64& n, int b) {
+  return __byte_perm(n.w[b >> 2], 0x4B000000u, (uint32_t)(b & 3) | 0x7540u);
+}
+
 // Child bound Origin + ldexpf(q, exp - 8) (asu.h:499-508) as one fused
 // multiply-add.  q * 2^(exp-8) is exact for an 8-bit q and exp in [-128, 127]
 // (at most 8 significant bits, all at or above 2^-149, below 2^127), so the
@@ -140,15 +181,21 @@ __device__ __forceinline__ ChildHits test_children(const Node64& n, uint32_t nod
   r.info = ((uint64_t)n.w[6] << 16) | (n.w[5] >> 16);  // bytes 22..27
   r.info &= 0x3f3f3f3f3f3full;
   r.child_unit = (uint32_t)((int)node_unit + child_off);
+  // x and y in two-wide FP32: the same roundings, fewer instructions
+  const unsigned long long s_xy = f2_pack(sx, sy), o_xy = f2_pack(ox, oy);
+  const unsigned long long org_xy = f2_pack(o.x, o.y), id_xy = f2_pack(idir.x, idir.y);
+  const unsigned long long two23 = f2_pack(8388608.0f, 8388608.0f);
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
     const uint32_t info = r.info_of(i);
     if (info & 3u) {
-      const float lx = (child_bound(n, rtf::IN_LO_X + i, ox, sx) - o.x) * idir.x;
-      const float ly = (child_bound(n, rtf::IN_LO_Y + i, oy, sy) - o.y) * idir.y;
+      // q as an exact float (bits - 2^23), Origin + q * 2^(e-8) fused, then (b - o) * idir
+      const unsigned long long qlo = f2_sub(f2_pack_bits(byte_bits(n, rtf::IN_LO_X + i), byte_bits(n, rtf::IN_LO_Y + i)), two23);
+      const unsigned long long qhi = f2_sub(f2_pack_bits(byte_bits(n, rtf::IN_HI_X + i), byte_bits(n, rtf::IN_HI_Y + i)), two23);
+      float lx, ly, hx, hy;
+      f2_unpack(f2_mul(f2_sub(f2_fma(qlo, s_xy, o_xy), org_xy), id_xy), lx, ly);
+      f2_unpack(f2_mul(f2_sub(f2_fma(qhi, s_xy, o_xy), org_xy), id_xy), hx, hy);
       const float lz = (child_bound(n, rtf::IN_LO_Z + i, oz, sz) - o.z) * idir.z;
-      const float hx = (child_bound(n, rtf::IN_HI_X + i, ox, sx) - o.x) * idir.x;
-      const float hy = (child_bound(n, rtf::IN_HI_Y + i, oy, sy) - o.y) * idir.y;
       const float hz = (child_bound(n, rtf::IN_HI_Z + i, oz, sz) - o.z) * idir.z;
       if (slab_hit<FAST>(lx, ly, lz, hx, hy, hz, tmin, tmax, cull)) r.hit_mask |= 1u << i;
     }
