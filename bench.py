@@ -200,15 +200,23 @@ TUNED = os.path.join(REPO, "treelet-prefetching-for-rt_gb300", "treelet_rt", "tu
 _tuned_cache = None
 
 
-def apply_tuning(scene, mode_name: str, batch: str) -> dict:
-    """Sets the autotuned launch parameters for (mode, batch kind), if tuned."""
+def _tuned(key: str):
+    """The autotuned entry for "mode/batch kind" (tuned_gb300.json), or None."""
     global _tuned_cache
     if _tuned_cache is None:
         _tuned_cache = {}
         if os.path.exists(TUNED):
             with open(TUNED) as f:
                 _tuned_cache = json.load(f).get("results", {})
-    r = _tuned_cache.get(f"{mode_name}/{batch}")
+    return _tuned_cache.get(key)
+
+
+def apply_tuning(scene, mode_name: str, batch: str) -> dict:
+    """Sets the autotuned launch parameters for (mode, batch kind), if tuned
+    (AO rays fall back to the bounce rays' entry)."""
+    r = _tuned(f"{mode_name}/{batch}")
+    if r is None and batch == "ao":
+        r = _tuned(f"{mode_name}/bounce")
     if r:
         scene.set_tuning(**r["tuning"])
         return r["tuning"]
@@ -591,7 +599,7 @@ def run_ao(args) -> None:
         info = scene.form_treelets(budget)
         row = {"treelets": info["n_treelets"]}
         for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
-            apply_tuning(scene, name, "bounce")
+            apply_tuning(scene, name, "ao")
             ms = _time_launch(lambda: scene.trace(d_ao, d_hits, mode, default_flags=flags, stream=sp, n=n),
                               max(3, args.steps), flush, stream)
             row[name] = round(n / ms / 1e3, 3)
@@ -608,6 +616,12 @@ def run_ao(args) -> None:
                        "l2": "flushed", "setup_s": round(setup, 1)},
             "budgets": table, "dtype": "f32", "data": "synthetic"}
     print(json.dumps(line), flush=True)
+
+
+def _tuned_batch(mode_name: str) -> dict:
+    """The autotuned batch-launch tuning for a mode (plain / treelet), if any."""
+    r = _tuned(f"{mode_name}/batch")
+    return r["tuning"] if r else {}
 
 
 def run_batch(args) -> None:
@@ -666,10 +680,12 @@ def run_batch(args) -> None:
     ray_bytes = d_rays.data_ptr()
     hit_bytes = d_hits2.data_ptr()
     out = {}
-    for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET)):
+    for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
         for s in scenes:
             apply_tuning(s, name, "bounce")
-        tuned = apply_tuning(scenes[0], name, "bounce")
+            if name == "staged":
+                s.set_tuning(queue_rounds=rt.TUNING_OFF)
+        tuned = _tuned_batch(name)
         if tuned:
             batch.set_tuning(**tuned)
 
@@ -730,11 +746,13 @@ def run_queues(args) -> None:
         row = {}
         for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET)):
             apply_tuning(scene, name, batch)
-            row[name] = round(n / _time_launch(lambda: scene.trace(d, hp, mode, stream=sp, n=n), max(3, args.steps),
+            _time_launch(lambda: scene.trace(d, hp, mode, stream=sp, n=n), 2, flush, stream)  # warm
+            row[name] = round(n / _time_launch(lambda: scene.trace(d, hp, mode, stream=sp, n=n), max(5, args.steps),
                                                flush, stream) / 1e3, 3)
         apply_tuning(scene, "staged", batch)
         for rounds in (rt.TUNING_OFF, 1, 2, 4, 8):
             scene.set_tuning(queue_rounds=rounds)
+            scene.trace(d, hp, rt.MODE_STAGED, stream=sp, n=n)  # the queues' memory is allocated here
             ms = _time_launch(lambda: scene.trace(d, hp, rt.MODE_STAGED, stream=sp, n=n), max(3, args.steps), flush,
                               stream)
             st = scene.stats()

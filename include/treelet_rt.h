@@ -368,9 +368,13 @@ rt_status rt_gen_bounce_rays(rt_scene* scene, const rt_ray* rays, const rt_hit* 
 /* A batch traces rays of many scenes in ONE persistent work-queue launch
  * (no reference counterpart: the reference traces one ray per call).  Item k
  * covers rays [ray_begin[k], ray_begin[k+1]) of the concatenated ray and hit
- * arrays and uses scenes[item_scene[k]].  Modes PLAIN and TREELET (every
- * scene needs rt_treelets_form for TREELET).  The batch owns its queue and
- * counter memory; the scenes must outlive it. */
+ * arrays and uses scenes[item_scene[k]].  Modes PLAIN and TREELET run as one
+ * launch over every item with the batch's tuning; RT_MODE_STAGED runs each
+ * item as its scene's own staged launch (its pinned treelets and tuning,
+ * without treelet queues), in item order on the stream, because a CTA's
+ * shared memory holds one scene's treelets.  TREELET and STAGED need
+ * rt_treelets_form on every scene.  The batch owns its queue and counter
+ * memory; the scenes must outlive it. */
 typedef struct rt_batch rt_batch;
 rt_status rt_batch_create(rt_ctx* ctx, rt_scene* const* scenes, uint32_t n_scenes, rt_batch** out);
 rt_status rt_batch_destroy(rt_batch* b);
@@ -379,7 +383,9 @@ rt_status rt_batch_set_tuning(rt_batch* b, const rt_tuning* t);
 rt_status rt_trace_batch(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                          uint32_t mode, rt_hit* hits, void* stream);
 /* Records rt_trace_batch with these buffers into a CUDA graph owned by the
- * batch (replacing any previous one); rt_batch_graph_launch replays it. */
+ * batch (replacing any previous one); rt_batch_graph_launch replays it.  For
+ * RT_MODE_STAGED the call first runs the batch once, uncaptured, so that every
+ * staged kernel's launch shape is set before recording. */
 rt_status rt_batch_graph_capture(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                                  uint32_t mode, rt_hit* hits, void* stream);
 rt_status rt_batch_graph_launch(rt_batch* b, void* stream);

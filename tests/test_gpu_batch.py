@@ -1,6 +1,7 @@
 """Many scenes in one persistent work-queue launch (and its CUDA-graph
 replay) give the same hit records as one rt_trace launch per scene, and the
-stack-depth variants agree."""
+stack-depth variants agree.  A staged batch runs each item as its scene's own
+staged launch, recorded in the same graph."""
 import numpy as np
 import pytest
 
@@ -25,13 +26,13 @@ def _scenes(ctx):
     return out
 
 
-@pytest.mark.parametrize("mode_name", ["plain", "treelet"])
+@pytest.mark.parametrize("mode_name", ["plain", "treelet", "staged"])
 def test_batch_matches_per_scene(ctx, mode_name):
     import torch
 
     import treelet_rt as rt
 
-    mode = rt.MODE_PLAIN if mode_name == "plain" else rt.MODE_TREELET
+    mode = {"plain": rt.MODE_PLAIN, "treelet": rt.MODE_TREELET, "staged": rt.MODE_STAGED}[mode_name]
     scenes = _scenes(ctx)
     # items interleave scenes and split some scenes' rays in two
     items, order = [], []

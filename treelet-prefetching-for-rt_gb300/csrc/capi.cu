@@ -768,7 +768,7 @@ rt_status check_trace(const rt_scene* s, uint32_t mode, const rt_trace_buf* trac
 // counter of this launch; `keep` adds the counters to the previous launch's.
 rt_status trace_launch(rt_scene* s, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t n,
                        uint32_t mode, rt_hit* hits, const rt_trace_buf* trace, cudaStream_t st, uint32_t* queue,
-                       bool keep) {
+                       bool keep, bool allow_queues = true) {
   rtk::TraceArgs a{};
   a.blob = reinterpret_cast<const uint4*>(s->d_blob);
   a.n_units = s->n_units;
@@ -794,7 +794,7 @@ rt_status trace_launch(rt_scene* s, const rt_ray* rays, const uint32_t* flags, u
   a.status = s->d_status;
   a.queue = queue;
   a.hint = s->d_hint;
-  if (queued(s, mode)) {
+  if (allow_queues && queued(s, mode)) {
     rt_status qst = ensure_queue_scratch(s, n);
     if (qst != RT_OK) return qst;
     return launch_trace(a, mode, s->tuning, s->slot_bytes, st, keep, &s->qs);
@@ -1178,6 +1178,7 @@ struct rt_batch {
   uint32_t* d_item_begin = nullptr;
   uint32_t* d_item_scene = nullptr;
   uint32_t n_items = 0, n_rays = 0;
+  std::vector<uint32_t> item_begin, item_scene;  // host copies (staged batches launch per item)
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;
@@ -1198,10 +1199,9 @@ void free_graph(rt_batch* b) {
 rt_status batch_args(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, uint32_t mode,
                      rt_hit* hits, rtk::TraceArgs& a) {
   if (!rays || !hits) return rti::fail(RT_ERR_INVALID, "rt_trace_batch: NULL rays or hits");
-  if (mode != RT_MODE_PLAIN && mode != RT_MODE_TREELET)
-    return rti::fail(RT_ERR_INVALID, "rt_trace_batch: batches run RT_MODE_PLAIN or RT_MODE_TREELET");
+  if (mode > RT_MODE_STAGED) return rti::fail(RT_ERR_INVALID, "rt_trace_batch: unknown mode");
   if (b->n_items == 0) return rti::fail(RT_ERR_STATE, "rt_trace_batch: call rt_batch_set_items first");
-  if (mode == RT_MODE_TREELET)
+  if (mode != RT_MODE_PLAIN)
     for (rt_scene* s : b->scenes)
       if (!s->has_treelets) return rti::fail(RT_ERR_STATE, "rt_trace_batch: a scene has no treelets");
   // scenes may have (re)formed their treelets since the views were uploaded
@@ -1232,6 +1232,26 @@ rt_status batch_args(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uin
   a.stats = b->d_stats;
   a.status = b->d_status;
   a.queue = b->d_queue;
+  return RT_OK;
+}
+
+// A staged batch: each item runs its scene's own staged walk (the scene's
+// pinned treelets in shared memory and its own tuning, without treelet
+// queues, whose memory a scene grows on demand), one launch per item in
+// order on `st`.  A CTA's shared memory holds one scene's treelets, so the
+// items are not merged into one persistent launch as the other modes are.
+rt_status batch_staged(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, rt_hit* hits,
+                       cudaStream_t st) {
+  for (uint32_t k = 0; k < b->n_items; ++k) {
+    const uint32_t lo = b->item_begin[k], m = b->item_begin[k + 1] - lo;
+    if (m == 0) continue;
+    rt_scene* s = b->scenes[b->item_scene[k]];
+    rt_status r = check_trace(s, RT_MODE_STAGED, nullptr, "rt_trace_batch");
+    if (r != RT_OK) return r;
+    r = trace_launch(s, rays + lo, flags ? flags + lo : nullptr, default_flags, m, RT_MODE_STAGED, hits + lo, nullptr,
+                     st, s->d_queue, false, false);
+    if (r != RT_OK) return r;
+  }
   return RT_OK;
 }
 
@@ -1306,6 +1326,8 @@ rt_status rt_batch_set_items(rt_batch* b, const uint32_t* ray_begin, const uint3
   RT_CUDA(cudaMemcpy(b->d_item_scene, item_scene, sizeof(uint32_t) * n_items, cudaMemcpyHostToDevice));
   b->n_items = n_items;
   b->n_rays = ray_begin[n_items];
+  b->item_begin.assign(ray_begin, ray_begin + n_items + 1);
+  b->item_scene.assign(item_scene, item_scene + n_items);
   return RT_OK;
 }
 
@@ -1326,6 +1348,7 @@ rt_status rt_trace_batch(rt_batch* b, const rt_ray* rays, const uint32_t* flags,
   if (st != RT_OK) return st;
   if (b->n_rays == 0) return RT_OK;
   RT_CUDA(cudaSetDevice(b->ctx->device));
+  if (mode == RT_MODE_STAGED) return batch_staged(b, rays, flags, default_flags, hits, (cudaStream_t)stream);
   return launch_trace(a, mode, b->tuning, 0, (cudaStream_t)stream);
 }
 
@@ -1339,9 +1362,15 @@ rt_status rt_batch_graph_capture(rt_batch* b, const rt_ray* rays, const uint32_t
   RT_CUDA(cudaSetDevice(b->ctx->device));
   free_graph(b);
   cudaStream_t s = (cudaStream_t)stream;
-  // the kernel attributes and launch shapes are resolved outside the capture
+  if (mode == RT_MODE_STAGED) {
+    // the staged kernels' shared-memory attributes and launch shapes are set
+    // by one launch of the batch outside the capture
+    st = batch_staged(b, rays, flags, default_flags, hits, s);
+    if (st != RT_OK) return st;
+    RT_CUDA(cudaStreamSynchronize(s));
+  }
   RT_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  st = launch_trace(a, mode, b->tuning, 0, s);
+  st = mode == RT_MODE_STAGED ? batch_staged(b, rays, flags, default_flags, hits, s) : launch_trace(a, mode, b->tuning, 0, s);
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(s, &g);
   if (st != RT_OK) {
