@@ -56,8 +56,8 @@ def test_ao_4m_triangles_sample_matches_oracle(ctx, blobs_scene, budget):
                                      (rt.MODE_STAGED, 1, "staged, queued", {"queue_rounds": 4})):
         if extra:
             scene.set_tuning(**extra)
-        oh, ov, ot = orc.trace(bb, ao, omode, tl if omode else None, default_flags=flags, capacity=cap,
-                               want_visits=True, want_treelets=True, threads=16)
+        oh, ov, ot = orc.trace(bb, ao, omode, tl, default_flags=flags, capacity=cap, want_visits=True,
+                               want_treelets=True, threads=16)
         hits, vis, tids = scene.trace_host(ao, mode, default_flags=flags, capacity=cap, want_visits=True,
                                            want_treelets=True)
         assert_hits_equal(hits, oh, f"{name} hits, budget {budget}")

@@ -52,7 +52,7 @@ def test_training_and_gain_over_heuristic(ctx):
     n_tl = info["n_treelets"]
     pop = L.popularity_table(train, n_tl)
     mlp = L.Mlp(ctx, n_tl, seed=1)
-    losses = L.train(mlp, train, steps=600, batch=4096, lr=3e-3, lr_final=3e-4)
+    losses = L.train(mlp, train, steps=3000, batch=4096, lr=3e-3, lr_final=3e-4)
     assert np.mean(losses[-50:]) < 0.7 * np.mean(losses[:50])
     pred = L.predict(mlp, test)
     h_pop = L.hit_rates(pop[test["current"]], test["target"])
@@ -74,3 +74,36 @@ def test_training_and_gain_over_heuristic(ctx):
     got, _, _ = scene.trace_host(rays, rt.MODE_STAGED)
     assert np.array_equal(got.view(np.uint8), ref.view(np.uint8))
     scene.close()
+
+
+def test_top4_matches_oracle_logits(ctx):
+    """rt_mlp_topk (the output layer's fused pass, no stored logits) against
+    the float64 oracle's logits: the same four treelets in the same order
+    wherever the five largest logits are not within BF16 noise of each
+    other."""
+    from oracle import mlp_oracle as mo
+    from treelet_rt import learned as L
+
+    C = 1500
+    mlp = L.Mlp(ctx, C, seed=3)
+    rng = np.random.default_rng(4)
+    p = mlp.get_params()
+    # spread the output weights so that logits differ clearly
+    offs = np.cumsum([0, C * 16, 22 * 64, 64, 64 * 64, 64, 64 * C, C])
+    p[offs[5]:offs[6]] = rng.normal(0, 4.0, offs[6] - offs[5])
+    p[offs[6]:offs[7]] = rng.normal(0, 2.0, C)
+    mlp.set_params(p)
+    n = 333
+    s = np.zeros(n, L.SAMPLE_DTYPE)
+    s["origin"] = rng.uniform(0, 1, (n, 3))
+    s["dir"] = rng.uniform(-1, 1, (n, 3))
+    s["current"] = rng.integers(0, C, n)
+    got = L.predict(mlp, s)
+    z = mo.logits(mlp.get_params(), s, C)
+    order = np.argsort(-z, axis=1, kind="stable")[:, :5]
+    top5 = np.take_along_axis(z, order, axis=1)
+    # BF16 rounding of the weights and activations moves a logit by about 0.05 here
+    clear = (np.diff(-top5, axis=1) > 0.3).all(axis=1)
+    assert clear.sum() > n // 4
+    assert np.array_equal(got[clear].astype(np.int64), order[clear, :4])
+    mlp.close()

@@ -7,10 +7,11 @@
 //   z  = h2 W3 + b3                                     one logit per treelet
 //
 // Weights are used in BF16 with FP32 accumulation; FP32 master copies are
-// what Adam updates.  The matrix products run on the tensor cores through
-// mma.sync m16n8k16 (BF16 in, FP32 accumulate): every product here has one
-// dimension of 64 or less, which the warp-level MMA covers without the
-// shared-memory staging and TMEM round trip a tcgen05 tile would need.
+// what Adam updates.  The output layer, whose products span every treelet,
+// runs on the fifth-generation tensor cores (tcgen05.mma with accumulators in
+// tensor memory) fused with the softmax cross-entropy, so the batch x
+// treelets logits are never stored (mlp_tc.cuh).  The two hidden layers
+// (4096 x 64 x 64 at most) run on mma.sync m16n8k16 tiles.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -19,6 +20,7 @@
 #include <vector>
 
 #include "capi_internal.h"
+#include "mlp_tc.cuh"
 
 namespace {
 
@@ -41,10 +43,6 @@ __device__ __forceinline__ float gelu_grad(float x) {
   const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
   const float pdf = 0.3989422804014327f * expf(-0.5f * x * x);
   return cdf + x * pdf;
-}
-
-__device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
 template <bool AT, bool BT, int EPI>
@@ -164,40 +162,6 @@ __global__ void gather_inputs(const rt_mlp_sample* __restrict__ s, int n, const 
   X[i] = __float2bfloat16(v);
 }
 
-// Per row: loss += (logsumexp(z) - z[target]) / n; dZ = (softmax(z) - onehot) / n.
-__global__ void softmax_xent(const float* __restrict__ Z, int n, int C, const rt_mlp_sample* __restrict__ s,
-                             bf16* __restrict__ dZ, float* __restrict__ loss) {
-  const int row = blockIdx.x;
-  const float* z = Z + (size_t)row * C;
-  __shared__ float red[32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  float mx = -INFINITY;
-  for (int j = tid; j < C; j += blockDim.x) mx = fmaxf(mx, z[j]);
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (lane == 0) red[warp] = mx;
-  __syncthreads();
-  mx = red[0];
-  for (int w = 1; w < nw; ++w) mx = fmaxf(mx, red[w]);
-  __syncthreads();
-  float sum = 0.0f;
-  for (int j = tid; j < C; j += blockDim.x) sum += expf(z[j] - mx);
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-  if (lane == 0) red[warp] = sum;
-  __syncthreads();
-  sum = 0.0f;
-  for (int w = 0; w < nw; ++w) sum += red[w];
-  const uint32_t tgt = s[row].target;
-  const float inv = 1.0f / sum, scale = 1.0f / (float)n;
-  if (dZ) {
-    bf16* d = dZ + (size_t)row * C;
-    for (int j = tid; j < C; j += blockDim.x) {
-      const float p = expf(z[j] - mx) * inv;
-      d[j] = __float2bfloat16((p - (j == (int)tgt ? 1.0f : 0.0f)) * scale);
-    }
-  }
-  if (tid == 0 && tgt < (uint32_t)C) atomicAdd(loss, (logf(sum) + mx - z[tgt]) * scale);
-}
-
 // dZ = dH * GELU'(Z) as BF16.
 __global__ void gelu_back(const float* __restrict__ dH, const float* __restrict__ Z, bf16* __restrict__ dZ, int count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -269,44 +233,6 @@ __global__ void init_params(float* __restrict__ p, uint64_t n, uint64_t seed, ui
   p[i] = v;
 }
 
-// One warp per row: the four largest logits (ties: lower index first).
-__global__ void topk4(const float* __restrict__ Z, int n, int C, uint32_t* __restrict__ out) {
-  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const float* z = Z + (size_t)row * C;
-  float v[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
-  int ix[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-  for (int j = lane; j < C; j += 32) {
-    const float x = z[j];
-    if (x > v[3] || (x == v[3] && j < ix[3])) {
-      int p = 3;
-      while (p > 0 && (x > v[p - 1] || (x == v[p - 1] && j < ix[p - 1]))) {
-        v[p] = v[p - 1];
-        ix[p] = ix[p - 1];
-        --p;
-      }
-      v[p] = x;
-      ix[p] = j;
-    }
-  }
-  int head = 0;
-  for (int k = 0; k < 4; ++k) {
-    float bv = head < 4 ? v[head] : -INFINITY;
-    int bi = head < 4 ? ix[head] : 0x7fffffff;
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > bv || (ov == bv && oi < bi)) {
-        bv = ov;
-        bi = oi;
-      }
-    }
-    if (head < 4 && ix[head] == bi) ++head;
-    if (lane == 0) out[(size_t)row * 4 + k] = (uint32_t)(bi == 0x7fffffff ? 0xFFFFFFFFu : bi);
-  }
-}
-
 }  // namespace
 
 struct rt_mlp {
@@ -314,9 +240,13 @@ struct rt_mlp {
   uint32_t C = 0;
   uint64_t n_params = 0, offW1 = 0, offb1 = 0, offW2 = 0, offb2 = 0, offW3 = 0, offb3 = 0;
   float *P = nullptr, *M = nullptr, *V = nullptr, *G = nullptr;
-  bf16 *E16 = nullptr, *W1_16 = nullptr, *W2_16 = nullptr, *W3_16 = nullptr;
-  bf16 *X = nullptr, *H1 = nullptr, *H2 = nullptr, *dZ3 = nullptr, *dZ2 = nullptr, *dZ1 = nullptr;
-  float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *dH2 = nullptr, *dH1 = nullptr, *dX = nullptr, *dW1 = nullptr;
+  bf16 *E16 = nullptr, *W1_16 = nullptr, *W2_16 = nullptr;
+  bf16 *W3T = nullptr, *W3P = nullptr, *H2X = nullptr;  // output-layer operands (mlp_tc.cuh)
+  uint32_t Cp = 0;                                     // treelets padded to the output chunk
+  bf16 *X = nullptr, *H1 = nullptr, *H2 = nullptr, *dZ2 = nullptr, *dZ1 = nullptr;
+  float *Z1 = nullptr, *Z2 = nullptr, *dH2 = nullptr, *dH1 = nullptr, *dX = nullptr, *dW1 = nullptr;
+  float *lse = nullptr, *part = nullptr;
+  uint32_t* tstatus = nullptr;                         // bit 0: a bounded wait of the output layer gave up
   float* loss = nullptr;
   uint64_t step = 0;
   cudaStream_t st = nullptr;
@@ -344,7 +274,65 @@ void refresh_bf16(rt_mlp* m) {
   to_bf16<<<blocks((uint64_t)m->C * EMB), 256, 0, m->st>>>(m->P, m->E16, (uint64_t)m->C * EMB);
   w1_to_bf16<<<blocks(XP * H), 256, 0, m->st>>>(m->P + m->offW1, m->W1_16);
   to_bf16<<<blocks(H * H), 256, 0, m->st>>>(m->P + m->offW2, m->W2_16, H * H);
-  to_bf16<<<blocks((uint64_t)H * m->C), 256, 0, m->st>>>(m->P + m->offW3, m->W3_16, (uint64_t)H * m->C);
+  tcm::w3_operands_kernel<<<blocks((uint64_t)H * m->Cp), 256, 0, m->st>>>(m->P + m->offW3, m->C, m->Cp, m->W3T,
+                                                                          m->W3P);
+}
+
+// Column splits of the row-tile passes of the output layer: about two CTAs
+// per SM over the row tiles of the batch.
+uint32_t out_splits(const rt_mlp* m, uint32_t n) {
+  const uint32_t tiles = (n + tcm::TM - 1) / tcm::TM, chunks = m->Cp / tcm::TN;
+  const uint32_t want = (2 * 152 + tiles - 1) / tiles;
+  return std::max<uint32_t>(1, std::min(chunks, want));
+}
+
+constexpr size_t kSmemStats = 16384 + 65536 + 2048;
+constexpr size_t kSmemDh2 = 16384 + 32768 + 65536 + 32768 + 1024;
+constexpr size_t kSmemDw3 = 32768 + 16384 + 65536 + 20480 + 1024;
+
+tcm::OutArgs out_args(rt_mlp* m, const rt_mlp_sample* s, uint32_t n) {
+  tcm::OutArgs a{};
+  a.h2 = m->H2;
+  a.h2x = m->H2X;
+  a.ldx = RT_MLP_MAX_BATCH;
+  a.w3t = m->W3T;
+  a.w3p = m->W3P;
+  a.b3 = m->P + m->offb3;
+  a.s = s;
+  a.n = n;
+  a.C = m->C;
+  a.cp = m->Cp;
+  a.splits = out_splits(m, n);
+  a.part = m->part;
+  a.lse = m->lse;
+  a.dh2 = m->dH2;
+  a.dw3 = m->G + m->offW3;
+  a.db3 = m->G + m->offb3;
+  a.status = m->tstatus;
+  return a;
+}
+
+// Loss (and lse per row) of the output layer for n samples, or with top4 set
+// the four largest logits of each sample instead.
+void output_forward(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, uint32_t* top4) {
+  const tcm::OutArgs a = out_args(m, s, n);
+  const dim3 grid((n + tcm::TM - 1) / tcm::TM, a.splits);
+  if (top4) {
+    tcm::out_stats_kernel<true><<<grid, 128, kSmemStats, m->st>>>(a);
+    tcm::out_top4_kernel<<<blocks(n), 256, 0, m->st>>>(m->part, a.splits, n, top4);
+    return;
+  }
+  tcm::out_stats_kernel<false><<<grid, 128, kSmemStats, m->st>>>(a);
+  tcm::out_lse_kernel<<<blocks(n), 256, 0, m->st>>>(m->part, a.splits, n, s, m->C, m->lse, m->loss);
+}
+
+// Gradients of the output layer: dW3, db3 into G, dH2 (zeroed first).
+void output_backward(rt_mlp* m, const rt_mlp_sample* s, uint32_t n) {
+  const tcm::OutArgs a = out_args(m, s, n);
+  tcm::h2x_kernel<<<blocks((uint64_t)tcm::HX * RT_MLP_MAX_BATCH), 256, 0, m->st>>>(m->H2, n, RT_MLP_MAX_BATCH,
+                                                                                   m->H2X);
+  tcm::out_dh2_kernel<<<dim3((n + tcm::TM - 1) / tcm::TM, a.splits), 128, kSmemDh2, m->st>>>(a);
+  tcm::out_dw3_kernel<<<m->Cp / tcm::TN, 128, kSmemDw3, m->st>>>(a);
 }
 
 int ksplit(int K, int tiles) {
@@ -355,26 +343,23 @@ int ksplit(int K, int tiles) {
 }
 
 // Forward (and, when grads is true, backward into G) for n samples.
-rt_status run(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, bool grads, bool loss_only_logits) {
-  const int B = (int)n, C = (int)m->C;
+rt_status run(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, bool grads, uint32_t* top4) {
+  const int B = (int)n;
   cudaStream_t st = m->st;
   gather_inputs<<<blocks((uint64_t)B * XP), 256, 0, st>>>(s, B, m->E16, m->C, m->X);
   gemm<false, false, EPI_BIAS_GELU>(B, H, XP, m->X, XP, m->W1_16, H, m->Z1, H, m->P + m->offb1, m->H1, 1, st);
   gemm<false, false, EPI_BIAS_GELU>(B, H, H, m->H1, H, m->W2_16, H, m->Z2, H, m->P + m->offb2, m->H2, 1, st);
-  gemm<false, false, EPI_BIAS>(B, C, H, m->H2, H, m->W3_16, C, m->Z3, C, m->P + m->offb3, nullptr, 1, st);
-  if (loss_only_logits) return RT_OK;
+  if (top4) {
+    output_forward(m, s, n, top4);
+    return RT_OK;
+  }
   MLP_CUDA(cudaMemsetAsync(m->loss, 0, sizeof(float), st));
-  softmax_xent<<<B, 256, 0, st>>>(m->Z3, B, C, s, grads ? m->dZ3 : nullptr, m->loss);
+  output_forward(m, s, n, nullptr);
   if (!grads) return RT_OK;
   MLP_CUDA(cudaMemsetAsync(m->G, 0, sizeof(float) * m->n_params, st));
-  // W3, b3
-  gemm<true, false, EPI_ACC>(H, C, B, m->H2, H, m->dZ3, C, m->G + m->offW3, C, nullptr, nullptr,
-                             ksplit(B, (C + 63) / 64), st);
-  col_sum<<<blocks(C), 256, 0, st>>>(m->dZ3, B, C, m->G + m->offb3);
-  // dH2 = dZ3 W3^T
+  // W3, b3 and dH2 = dz W3^T, on the tensor cores without the logits
   MLP_CUDA(cudaMemsetAsync(m->dH2, 0, sizeof(float) * B * H, st));
-  gemm<false, true, EPI_ACC>(B, H, C, m->dZ3, C, m->W3_16, C, m->dH2, H, nullptr, nullptr,
-                             ksplit(C, (B + 63) / 64), st);
+  output_backward(m, s, n);
   gelu_back<<<blocks((uint64_t)B * H), 256, 0, st>>>(m->dH2, m->Z2, m->dZ2, B * H);
   // W2, b2
   gemm<true, false, EPI_ACC>(H, H, B, m->H1, H, m->dZ2, H, m->G + m->offW2, H, nullptr, nullptr, ksplit(B, 1), st);
@@ -393,6 +378,16 @@ rt_status run(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, bool grads, bool lo
   gemm<false, true, EPI_ACC>(B, XP, H, m->dZ1, H, m->W1_16, H, m->dX, XP, nullptr, nullptr, 1, st);
   embed_grad<<<blocks((uint64_t)B * EMB), 256, 0, st>>>(m->dX, s, B, m->C, m->G);
   return RT_OK;
+}
+
+// After the stream has been synchronised: RT_ERR_TIMEOUT (and the flag
+// cleared) if a bounded wait of the output layer gave up.
+rt_status check_status(rt_mlp* m, const char* who) {
+  uint32_t st = 0;
+  MLP_CUDA(cudaMemcpy(&st, m->tstatus, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st == 0) return RT_OK;
+  MLP_CUDA(cudaMemset(m->tstatus, 0, sizeof(uint32_t)));
+  return rti::fail(RT_ERR_TIMEOUT, std::string(who) + ": a bounded tensor-core wait gave up; results are invalid");
 }
 
 }  // namespace
@@ -427,22 +422,31 @@ rt_status rt_mlp_create(rt_ctx* ctx, uint32_t n_treelets, uint64_t seed, rt_mlp*
   chk(mk(&m->E16, C * EMB));
   chk(mk(&m->W1_16, XP * H));
   chk(mk(&m->W2_16, H * H));
-  chk(mk(&m->W3_16, H * C));
+  m->Cp = (uint32_t)((C + tcm::TN - 1) / tcm::TN * tcm::TN);
+  chk(mk(&m->W3T, (size_t)m->Cp * H));
+  chk(mk(&m->W3P, (size_t)m->Cp * H));
+  chk(mk(&m->H2X, (size_t)tcm::HX * MB));
   chk(mk(&m->X, MB * XP));
   chk(mk(&m->H1, MB * H));
   chk(mk(&m->H2, MB * H));
-  chk(mk(&m->dZ3, MB * C));
   chk(mk(&m->dZ2, MB * H));
   chk(mk(&m->dZ1, MB * H));
   chk(mk(&m->Z1, MB * H));
   chk(mk(&m->Z2, MB * H));
-  chk(mk(&m->Z3, MB * C));
+  chk(mk(&m->lse, MB));
+  chk(mk(&m->part, 8 * 152 * 2 * MB));  // the largest split count times 8 floats per row
+  chk(mk(&m->tstatus, 1));
   chk(mk(&m->dH2, MB * H));
   chk(mk(&m->dH1, MB * H));
   chk(mk(&m->dX, MB * XP));
   chk(mk(&m->dW1, XP * H));
   chk(mk(&m->loss, 1));
   chk(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
+  chk(cudaFuncSetAttribute(tcm::out_stats_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemStats));
+  chk(cudaFuncSetAttribute(tcm::out_stats_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemStats));
+  chk(cudaFuncSetAttribute(tcm::out_dh2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDh2));
+  chk(cudaFuncSetAttribute(tcm::out_dw3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDw3));
+  if (e == cudaSuccess) e = cudaMemset(m->tstatus, 0, sizeof(uint32_t));
   if (e != cudaSuccess) {
     rt_mlp_destroy(m);
     return rti::fail(RT_ERR_OOM, std::string("rt_mlp_create: ") + cudaGetErrorString(e));
@@ -464,8 +468,9 @@ rt_status rt_mlp_create(rt_ctx* ctx, uint32_t n_treelets, uint64_t seed, rt_mlp*
 rt_status rt_mlp_destroy(rt_mlp* m) {
   if (!m) return RT_OK;
   cudaSetDevice(m->device);
-  void* ptrs[] = {m->P, m->M, m->V, m->G, m->E16, m->W1_16, m->W2_16, m->W3_16, m->X, m->H1, m->H2, m->dZ3,
-                  m->dZ2, m->dZ1, m->Z1, m->Z2, m->Z3, m->dH2, m->dH1, m->dX, m->dW1, m->loss};
+  void* ptrs[] = {m->P, m->M, m->V, m->G, m->E16, m->W1_16, m->W2_16, m->W3T, m->W3P, m->H2X, m->X, m->H1,
+                  m->H2, m->dZ2, m->dZ1, m->Z1, m->Z2, m->dH2, m->dH1, m->dX, m->dW1, m->lse, m->part,
+                  m->tstatus, m->loss};
   for (void* p : ptrs) cudaFree(p);
   if (m->st) cudaStreamDestroy(m->st);
   delete m;
@@ -500,10 +505,12 @@ rt_status rt_mlp_loss_grad(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, float*
   if (!m || !s || n == 0) return rti::fail(RT_ERR_INVALID, "rt_mlp_loss_grad: bad argument");
   if (n > RT_MLP_MAX_BATCH) return rti::fail(RT_ERR_TOO_LARGE, "rt_mlp_loss_grad: batch above RT_MLP_MAX_BATCH");
   MLP_CUDA(cudaSetDevice(m->device));
-  rt_status st = run(m, s, n, grads_host != nullptr, false);
+  rt_status st = run(m, s, n, grads_host != nullptr, nullptr);
   if (st != RT_OK) return st;
   MLP_CUDA(cudaGetLastError());
   MLP_CUDA(cudaStreamSynchronize(m->st));
+  st = check_status(m, "rt_mlp_loss_grad");
+  if (st != RT_OK) return st;
   if (loss) MLP_CUDA(cudaMemcpy(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost));
   if (grads_host) MLP_CUDA(cudaMemcpy(grads_host, m->G, sizeof(float) * m->n_params, cudaMemcpyDeviceToHost));
   return RT_OK;
@@ -513,7 +520,7 @@ rt_status rt_mlp_train_step(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, float
   if (!m || !s || n == 0) return rti::fail(RT_ERR_INVALID, "rt_mlp_train_step: bad argument");
   if (n > RT_MLP_MAX_BATCH) return rti::fail(RT_ERR_TOO_LARGE, "rt_mlp_train_step: batch above RT_MLP_MAX_BATCH");
   MLP_CUDA(cudaSetDevice(m->device));
-  rt_status st = run(m, s, n, true, false);
+  rt_status st = run(m, s, n, true, nullptr);
   if (st != RT_OK) return st;
   m->step += 1;
   const float c1 = 1.0f - powf(0.9f, (float)m->step), c2 = 1.0f - powf(0.999f, (float)m->step);
@@ -523,6 +530,7 @@ rt_status rt_mlp_train_step(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, float
   if (loss) {
     MLP_CUDA(cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->st));
     MLP_CUDA(cudaStreamSynchronize(m->st));
+    return check_status(m, "rt_mlp_train_step");
   }
   return RT_OK;
 }
@@ -532,13 +540,12 @@ rt_status rt_mlp_topk(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, uint32_t* t
   MLP_CUDA(cudaSetDevice(m->device));
   for (uint32_t b0 = 0; b0 < n; b0 += RT_MLP_MAX_BATCH) {
     const uint32_t nb = std::min<uint32_t>(RT_MLP_MAX_BATCH, n - b0);
-    rt_status st = run(m, s + b0, nb, false, true);
+    rt_status st = run(m, s + b0, nb, false, top4 + (size_t)b0 * 4);
     if (st != RT_OK) return st;
-    topk4<<<blocks(nb, 8), 256, 0, m->st>>>(m->Z3, (int)nb, (int)m->C, top4 + (size_t)b0 * 4);
   }
   MLP_CUDA(cudaGetLastError());
   MLP_CUDA(cudaStreamSynchronize(m->st));
-  return RT_OK;
+  return check_status(m, "rt_mlp_topk");
 }
 
 }  // extern "C"
