@@ -337,12 +337,26 @@ def run_gpu(args, rank: int, world: int) -> None:
     d_vis = torch.empty(n_prim * TRACE_CAP, dtype=torch.int32, device=cuda)
     d_tl = torch.empty(n_prim * TRACE_CAP, dtype=torch.int32, device=cuda)
 
+    try:
+        from torch.cuda import nvtx
+
+        nvtx.range_push("setup")
+        nvtx.range_pop()
+    except Exception:  # a torch built without NVTX: no ranges
+        nvtx = None
+
     def launch(mode, rays_d, hits_d, batch, traced):
         apply_tuning(scene, names[mode], batch)
+        # an NVTX range per launch ("staged_bounce", "plain_traced_primary", ...)
+        # lets a profiler pick one walk: ncu --nvtx --nvtx-include "<name>/"
+        if nvtx:
+            nvtx.range_push(f"{names[mode]}{'_traced' if traced else ''}_{batch}")
         if traced:
             scene.trace(rays_d, hits_d, mode, visits=d_vis, treelets=d_tl, capacity=TRACE_CAP, stream=sp, n=n_prim)
         else:
             scene.trace(rays_d, hits_d, mode, stream=sp, n=n_prim)
+        if nvtx:
+            nvtx.range_pop()
 
     def step(mode, traced=False):
         launch(mode, d_prim, d_hits_p, "primary", traced)
@@ -462,7 +476,34 @@ def run_gpu(args, rank: int, world: int) -> None:
     import ctypes
 
     e2e_traced = e2e_rate(ctypes.byref(tb), 3)
-    del h_vis, h_tl
+
+    # the same traces packed (rt_trace_host_packed): only each ray's used
+    # entries cross to the host, behind per-ray offsets
+    h_off = torch.empty((n_prim + 1) * 8, dtype=torch.uint8).pin_memory()
+    packed_total = [0, 0]
+
+    def host_trace_packed(hr, batch):
+        apply_tuning(scene, "staged", batch)
+        got = ctypes.c_uint64(0)
+        check(lib().rt_trace_host_packed(scene.handle, hr.data_ptr(), None, rt.RAY_FLAG_OPAQUE, n_prim,
+                                         rt.MODE_STAGED, TRACE_CAP, h_hits.data_ptr(), h_off.data_ptr(),
+                                         h_vis.data_ptr(), h_tl.data_ptr(), n_prim * TRACE_CAP, ctypes.byref(got)))
+        packed_total[0 if batch == "primary" else 1] = got.value
+
+    for _ in range(max(1, args.warmup)):
+        host_trace_packed(h_prim, "primary")
+        host_trace_packed(h_bounce, "bounce")
+    tt = []
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        host_trace_packed(h_prim, "primary")
+        host_trace_packed(h_bounce, "bounce")
+        tt.append(time.perf_counter() - t)
+    e2e_packed = n_rays / (sum(tt) / len(tt)) / 1e6 * world
+    packed_d2h = n_rays * 64 + 2 * (n_prim + 1) * 8 + 2 * 4 * sum(packed_total)
+    del h_vis, h_tl, h_off
 
     # CPU baseline and parity sample: the reference's own traceRay over a
     # bounded sample of the same rays (primary rays spread over the frame and
@@ -524,7 +565,10 @@ def run_gpu(args, rank: int, world: int) -> None:
             "e2e": {"value": round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n_rays * 32,
                     "d2h_bytes_per_step": n_rays * 64,
                     "traced": {"value": round(e2e_traced, 3), "unit": "Mrays/s", "h2d_bytes_per_step": n_rays * 32,
-                               "d2h_bytes_per_step": n_rays * (64 + 2 * 4 * TRACE_CAP)}},
+                               "d2h_bytes_per_step": n_rays * (64 + 2 * 4 * TRACE_CAP)},
+                    "traced_packed": {"value": round(e2e_packed, 3), "unit": "Mrays/s",
+                                      "h2d_bytes_per_step": n_rays * 32, "d2h_bytes_per_step": int(packed_d2h),
+                                      "trace_entries_per_step": int(sum(packed_total))}},
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,
         }
@@ -685,9 +729,12 @@ def run_batch(args) -> None:
             apply_tuning(s, name, "bounce")
             if name == "staged":
                 s.set_tuning(queue_rounds=rt.TUNING_OFF)
-        tuned = _tuned_batch(name)
-        if tuned:
-            batch.set_tuning(**tuned)
+        # the batch's own tuned entry, else the scenes' bounce tuning (the
+        # same stack depth as the per-scene launches it is compared with)
+        tuned = _tuned_batch(name) or apply_tuning(scenes[0], name, "bounce")
+        if tuned and name != "staged":
+            batch.set_tuning(**{k: v for k, v in tuned.items() if k in ("block_threads", "refill_lanes",
+                                                                         "stack_depth")})
 
         def per_scene():
             for i, s in enumerate(scenes):

@@ -261,6 +261,22 @@ rt_status rt_trace(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, u
 rt_status rt_trace_host(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                         uint32_t n, uint32_t mode, rt_hit* hits, const rt_trace_buf* trace);
 
+/* rt_trace_host with the access traces packed: ray r's transactions are
+ * entries offsets[r] .. offsets[r+1]-1 of `visits` / `treelets` (either may be
+ * NULL, not both), its first min(n_visits, row_capacity) transactions in
+ * order, as the reference keeps one variable-length access list per ray
+ * (the per-thread transaction lists that traceRayWithTreelets fills,
+ * vulkan_ray_tracing.cc:2256-2262).  Only the used entries cross PCIe/C2C,
+ * not n x row_capacity.  `offsets` holds n + 1 entries; `capacity` is the
+ * entries `visits` and `treelets` each hold.  *total receives the entries
+ * written; when it exceeds `capacity`, hits, offsets and *total are still
+ * filled, the arrays are left alone and the call returns RT_ERR_TOO_LARGE
+ * (call again with arrays of *total entries).  n x row_capacity must stay
+ * below 2^32 and n at most 2^24.  Synchronous. */
+rt_status rt_trace_host_packed(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
+                               uint32_t n, uint32_t mode, uint32_t row_capacity, rt_hit* hits, uint64_t* offsets,
+                               uint32_t* visits, uint32_t* treelets, uint64_t capacity, uint64_t* total);
+
 /* rt_trace_host for callers that cannot allocate device memory: no
  * counterpart in the reference.  A simulator calling the traversal per warp
  * from its cycle loop, or a process whose device memory belongs to its own

@@ -78,9 +78,9 @@ def test_training_and_gain_over_heuristic(ctx):
 
 def test_top4_matches_oracle_logits(ctx):
     """rt_mlp_topk (the output layer's fused pass, no stored logits) against
-    the float64 oracle's logits: the same four treelets in the same order
-    wherever the five largest logits are not within BF16 noise of each
-    other."""
+    the float64 oracle's logits: four distinct treelets whose logits are,
+    rank by rank, the four largest within BF16 noise, and exactly the
+    oracle's four in its order wherever the five largest are clearly apart."""
     from oracle import mlp_oracle as mo
     from treelet_rt import learned as L
 
@@ -91,19 +91,26 @@ def test_top4_matches_oracle_logits(ctx):
     # spread the output weights so that logits differ clearly
     offs = np.cumsum([0, C * 16, 22 * 64, 64, 64 * 64, 64, 64 * C, C])
     p[offs[5]:offs[6]] = rng.normal(0, 4.0, offs[6] - offs[5])
-    p[offs[6]:offs[7]] = rng.normal(0, 2.0, C)
+    p[offs[6]:offs[7]] = rng.normal(0, 8.0, C)
     mlp.set_params(p)
     n = 333
     s = np.zeros(n, L.SAMPLE_DTYPE)
     s["origin"] = rng.uniform(0, 1, (n, 3))
     s["dir"] = rng.uniform(-1, 1, (n, 3))
     s["current"] = rng.integers(0, C, n)
-    got = L.predict(mlp, s)
+    got = L.predict(mlp, s).astype(np.int64)
     z = mo.logits(mlp.get_params(), s, C)
     order = np.argsort(-z, axis=1, kind="stable")[:, :5]
     top5 = np.take_along_axis(z, order, axis=1)
-    # BF16 rounding of the weights and activations moves a logit by about 0.05 here
-    clear = (np.diff(-top5, axis=1) > 0.3).all(axis=1)
-    assert clear.sum() > n // 4
-    assert np.array_equal(got[clear].astype(np.int64), order[clear, :4])
+    # BF16 rounding of the weights and activations moves a logit by about
+    # 0.05 here; 0.25 bounds it with room to spare
+    tol = 0.25
+    assert (np.sort(got, axis=1)[:, 1:] != np.sort(got, axis=1)[:, :-1]).all(), "repeated treelet in a top 4"
+    z_got = np.take_along_axis(z, got, axis=1)
+    assert (np.abs(z_got - top5[:, :4]) <= tol).all(), np.abs(z_got - top5[:, :4]).max()
+    clear = (np.diff(-top5, axis=1) > 2 * tol).all(axis=1)
+    assert clear.sum() >= 10, clear.sum()
+    assert np.array_equal(got[clear], order[clear, :4])
+    first = -np.diff(top5[:, :2], axis=1)[:, 0] > 2 * tol
+    assert first.sum() > n // 2 and np.array_equal(got[first, 0], order[first, 0])
     mlp.close()

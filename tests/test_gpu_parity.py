@@ -401,3 +401,52 @@ def test_walks_match_reference_golden(ctx, case, sname, rname, walk, flags, budg
         bad = np.nonzero((got != want).any(axis=1))[0]
         assert len(bad) == 0, (case, mode, "rays differing from the reference:", bad[:10])
     scene.close()
+
+
+@pytest.mark.parametrize("cap", [6, 48])
+def test_packed_host_traces_match_oracle(ctx, cap):
+    """rt_trace_host_packed returns each ray's first min(n_visits, cap)
+    transactions back to back: offsets, visit and treelet entries must equal
+    the oracle's rows cut to the same lengths, for every walk, including rays
+    whose traces overflow the row capacity; arrays too small for the traces
+    give RT_ERR_TOO_LARGE with hits, offsets and the total still filled."""
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 8192, 12)
+    prim = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 48, 48, 1, 1, 1e-4, 1e30)
+    ph, _, _ = orc.trace(blob.bytes(), prim, 0, threads=8)
+    rays = np.concatenate([prim, rt.bounce_rays_host(blob, prim, ph, seed=5), edge_rays()])
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(4096)
+    tl = orc.Treelets(blob.bytes(), 4096)
+    for mode, omode, name in _modes():
+        oh, ov, ot = orc.trace(blob.bytes(), rays, omode, tl, capacity=cap, want_visits=True, want_treelets=True,
+                               threads=8)
+        hits, off, vis, tids = scene.trace_host_packed(rays, mode, row_capacity=cap, want_visits=True,
+                                                       want_treelets=True, capacity=len(rays))
+        assert_hits_equal(hits, oh, f"{name} hits")
+        keep = np.minimum(oh["n_visits"], cap).astype(np.uint64)
+        assert off[0] == 0 and (np.diff(off) == keep).all(), name
+        mask = np.arange(cap)[None, :] < keep[:, None]
+        assert np.array_equal(vis, ov[mask]), f"{name} packed visits"
+        assert np.array_equal(tids, ot[mask]), f"{name} packed treelet ids"
+        if cap == 6:
+            assert (oh["status"] & rt.RAY_TRACE_OVERFLOW).any()
+    # one array only, and too small a capacity
+    total = int(off[-1])
+    hits, off2, vis, tids = scene.trace_host_packed(rays, rt.MODE_PLAIN, row_capacity=cap, want_visits=True,
+                                                    want_treelets=False, capacity=total - 1)
+    assert tids is None and len(vis) == int(off2[-1])
+    import ctypes as C
+
+    h = np.zeros(len(rays), rt.HIT_DTYPE)
+    o = np.zeros(len(rays) + 1, np.uint64)
+    v = np.zeros(max(total - 1, 1), np.uint32)
+    got = C.c_uint64(0)
+    st = rt.lib().rt_trace_host_packed(scene.handle, rays.ctypes.data, None, rt.RAY_FLAG_OPAQUE, len(rays),
+                                       rt.MODE_TREELET, cap, h.ctypes.data, o.ctypes.data, v.ctypes.data, None,
+                                       total - 1, C.byref(got))
+    assert st == rt.RT_ERR_TOO_LARGE and got.value == total == int(o[-1])
+    assert not v.any()
+    scene.close()

@@ -144,6 +144,8 @@ struct rt_scene {
   cudaEvent_t ev_in[rti::kHostChunks] = {}, ev_done[rti::kHostChunks] = {};
   void* d_io = nullptr;
   size_t io_bytes = 0;
+  void* d_pack = nullptr;  // packed access traces of rt_trace_host_packed
+  size_t pack_bytes = 0;
   rti::QueueScratch qs;  // treelet queues of RT_MODE_STAGED with queue_rounds
 };
 
@@ -597,6 +599,7 @@ rt_status rt_scene_destroy(rt_scene* s) {
   cudaFree(s->d_status);
   cudaFree(s->d_queue);
   cudaFree(s->d_io);
+  cudaFree(s->d_pack);
   cudaFree(s->qs.base);
   for (uint32_t c = 0; c < rti::kHostChunks; ++c) {
     if (s->ev_in[c]) cudaEventDestroy(s->ev_in[c]);
@@ -1391,3 +1394,152 @@ rt_status rt_batch_graph_launch(rt_batch* b, void* stream) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ packed traces
+namespace {
+
+// Transactions each ray keeps in its trace row: min(n_visits, row capacity).
+__global__ void trace_counts_kernel(const rt_hit* __restrict__ hits, uint32_t n, uint32_t cap,
+                                    uint32_t* __restrict__ counts) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) counts[r] = min(hits[r].n_visits, cap);
+}
+
+// offsets[r] = the totals of the scan blocks before r's + r's offset within
+// its block; offsets[n] = the total.
+__global__ void trace_offsets_kernel(const uint32_t* __restrict__ local, const uint32_t* __restrict__ block_sum,
+                                     const rt_hit* __restrict__ hits, uint32_t n, uint32_t cap,
+                                     unsigned long long* __restrict__ offsets) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) offsets[r] = (unsigned long long)block_sum[r / rtk::kBinScanItems] + local[r];
+  if (r == n - 1)
+    offsets[n] = (unsigned long long)block_sum[r / rtk::kBinScanItems] + local[r] + min(hits[r].n_visits, cap);
+}
+
+// One warp per ray copies the used prefix of its trace rows to its place in
+// the packed arrays.
+__global__ void trace_pack_kernel(const uint32_t* __restrict__ vis_rows, const uint32_t* __restrict__ tl_rows,
+                                  const unsigned long long* __restrict__ offsets, uint32_t n, uint32_t cap,
+                                  uint32_t* __restrict__ vis, uint32_t* __restrict__ tl) {
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t r = warp; r < n; r += warps) {
+    const unsigned long long o = offsets[r];
+    const uint32_t m = (uint32_t)(offsets[r + 1] - o);
+    for (uint32_t j = lane; j < m; j += 32) {
+      if (vis_rows) vis[o + j] = vis_rows[(uint64_t)r * cap + j];
+      if (tl_rows) tl[o + j] = tl_rows[(uint64_t)r * cap + j];
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const uint32_t* flags,
+                                          uint32_t default_flags, uint32_t n, uint32_t mode, uint32_t row_capacity,
+                                          rt_hit* hits, uint64_t* offsets, uint32_t* visits, uint32_t* treelets,
+                                          uint64_t capacity, uint64_t* total) {
+  if (!s) return rti::fail(RT_ERR_INVALID, "rt_trace_host_packed: NULL scene");
+  if (total) *total = 0;
+  if (n == 0) {
+    if (offsets) offsets[0] = 0;
+    return RT_OK;
+  }
+  if (!rays || !hits || !offsets || !total) return rti::fail(RT_ERR_INVALID, "rt_trace_host_packed: NULL argument");
+  if (row_capacity == 0 || (!visits && !treelets))
+    return rti::fail(RT_ERR_INVALID, "rt_trace_host_packed: no trace asked for (row_capacity 0 or no arrays)");
+  if ((uint64_t)n * row_capacity >= (1ull << 32))
+    return rti::fail(RT_ERR_TOO_LARGE, "rt_trace_host_packed: rays x row_capacity must stay below 2^32");
+  if ((uint64_t)n > (uint64_t)rtk::kBinScanItems * rtk::kBinScanItems)
+    return rti::fail(RT_ERR_TOO_LARGE, "rt_trace_host_packed: at most 2^24 rays per call");
+  // only the pointers' presence matters to the argument check
+  uint32_t mark = 0;
+  const rt_trace_buf probe{visits ? &mark : nullptr, treelets ? &mark : nullptr, row_capacity};
+  rt_status st = check_trace(s, mode, &probe, "rt_trace_host_packed");
+  if (st != RT_OK) return st;
+  RT_CUDA(cudaSetDevice(s->ctx->device));
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const uint32_t n_blocks = (n + rtk::kBinScanItems - 1) / rtk::kBinScanItems;
+  const size_t b_rays = al(sizeof(rt_ray) * (size_t)n), b_flags = flags ? al(sizeof(uint32_t) * (size_t)n) : 0;
+  const size_t b_hits = al(sizeof(rt_hit) * (size_t)n), b_row = al(sizeof(uint32_t) * (size_t)n * row_capacity);
+  const size_t b_cnt = al(sizeof(uint32_t) * (size_t)n), b_blk = al(sizeof(uint32_t) * rtk::kBinScanItems);
+  const size_t b_off = al(sizeof(unsigned long long) * ((size_t)n + 1));
+  const size_t need =
+      b_rays + b_flags + b_hits + (visits ? b_row : 0) + (treelets ? b_row : 0) + 2 * b_cnt + b_blk + b_off;
+  if (need > s->io_bytes) {
+    cudaFree(s->d_io);
+    s->d_io = nullptr;
+    s->io_bytes = 0;
+    st = dalloc((uint8_t**)&s->d_io, need);
+    if (st != RT_OK) return st;
+    s->io_bytes = need;
+  }
+  uint8_t* p = (uint8_t*)s->d_io;
+  auto take = [&](size_t b) {
+    uint8_t* r = p;
+    p += b;
+    return r;
+  };
+  rt_ray* d_rays = (rt_ray*)take(b_rays);
+  uint32_t* d_flags = flags ? (uint32_t*)take(b_flags) : nullptr;
+  rt_hit* d_hits = (rt_hit*)take(b_hits);
+  uint32_t* d_vis = visits ? (uint32_t*)take(b_row) : nullptr;
+  uint32_t* d_tl = treelets ? (uint32_t*)take(b_row) : nullptr;
+  uint32_t* d_cnt = (uint32_t*)take(b_cnt);
+  uint32_t* d_loc = (uint32_t*)take(b_cnt);
+  uint32_t* d_blk = (uint32_t*)take(b_blk);
+  unsigned long long* d_off = (unsigned long long*)take(b_off);
+  cudaStream_t cs = s->stream;
+  cudaError_t e = cudaMemcpyAsync(d_rays, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess && flags)
+    e = cudaMemcpyAsync(d_flags, flags, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, cs);
+  if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
+  rt_trace_buf rows{d_vis, d_tl, row_capacity};
+  st = trace_launch(s, d_rays, d_flags, default_flags, n, mode, d_hits, &rows, cs, s->d_queue, false);
+  if (st != RT_OK) return host_finish(s, st);
+  trace_counts_kernel<<<(n + 255) / 256, 256, 0, cs>>>(d_hits, n, row_capacity, d_cnt);
+  rtk::bin_scan_kernel<<<n_blocks, 1024, 0, cs>>>(d_cnt, d_loc, d_blk, n);
+  rtk::bin_scan_top_kernel<<<1, 1024, 0, cs>>>(d_blk, n_blocks);
+  trace_offsets_kernel<<<(n + 255) / 256, 256, 0, cs>>>(d_loc, d_blk, d_hits, n, row_capacity, d_off);
+  e = cudaGetLastError();
+  unsigned long long tot = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot, d_off + n, sizeof(tot), cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+  if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
+  *total = tot;
+  e = cudaMemcpyAsync(hits, d_hits, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(offsets, d_off, sizeof(unsigned long long) * ((size_t)n + 1), cudaMemcpyDeviceToHost, cs);
+  if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
+  if (tot > capacity) {
+    st = host_finish(s, RT_OK);
+    if (st != RT_OK) return st;
+    return rti::fail(RT_ERR_TOO_LARGE, "rt_trace_host_packed: " + std::to_string(tot) +
+                                           " trace entries exceed the arrays' capacity (hits and offsets are filled)");
+  }
+  const size_t b_pack = al(sizeof(uint32_t) * (size_t)tot);
+  const size_t pack_need = (visits ? b_pack : 0) + (treelets ? b_pack : 0) + 256;
+  if (pack_need > s->pack_bytes) {
+    e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
+    cudaFree(s->d_pack);
+    s->d_pack = nullptr;
+    s->pack_bytes = 0;
+    st = dalloc((uint8_t**)&s->d_pack, pack_need);
+    if (st != RT_OK) return host_finish(s, st);
+    s->pack_bytes = pack_need;
+  }
+  uint32_t* p_vis = visits ? (uint32_t*)s->d_pack : nullptr;
+  uint32_t* p_tl = treelets ? (uint32_t*)((uint8_t*)s->d_pack + (visits ? b_pack : 0)) : nullptr;
+  if (tot > 0) {
+    trace_pack_kernel<<<std::min<uint32_t>((n + 7) / 8, 152 * 16), 256, 0, cs>>>(d_vis, d_tl, d_off, n, row_capacity,
+                                                                                  p_vis, p_tl);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && visits)
+      e = cudaMemcpyAsync(visits, p_vis, sizeof(uint32_t) * (size_t)tot, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess && treelets)
+      e = cudaMemcpyAsync(treelets, p_tl, sizeof(uint32_t) * (size_t)tot, cudaMemcpyDeviceToHost, cs);
+    if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
+  }
+  return host_finish(s, RT_OK);
+}

@@ -20,7 +20,7 @@ from ._ffi import (HIT_DTYPE, MODE_PLAIN, MODE_STAGED, MODE_TREELET, NO_TREELET,
                    SCENE_SHARED_BLAS, SCENE_TERRAIN_INSTANCES, TX_BYTES, TX_NAMES, Camera, PrefetchParams,
                    TUNING_OFF, PF_CLASSES, UNIT_PF_NONE, UNIT_PF_STRIDE, UNIT_PF_TREELET, UNIT_SCHED_FIRST,
                    UNIT_SCHED_OMR, UNIT_SCHED_PMR, UNIT_STATS_DTYPE, PinnedInfo, RTError, TraceBuf, TraceStats,
-                   TreeletInfo, Tuning, UnitConfig, check, lib, ptr, unit_config)
+                   TreeletInfo, Tuning, UnitConfig, RT_ERR_TOO_LARGE, check, lib, ptr, unit_config)
 
 __all__ = [
     "Blob", "Context", "Scene", "camera_rays", "default_camera", "bounce_rays_host", "RTError", "lib",
@@ -320,6 +320,35 @@ class Scene:
         check(lib().rt_trace_host(self._h, rays.ctypes.data, ptr(fl), default_flags, n, mode, hits.ctypes.data,
                                   C.byref(tb) if (want_visits or want_treelets) else None))
         return hits, vis, tl
+
+    def trace_host_packed(self, rays: np.ndarray, mode: int = MODE_PLAIN, flags=None,
+                          default_flags: int = RAY_FLAG_OPAQUE, row_capacity: int = 64, want_visits: bool = True,
+                          want_treelets: bool = False, capacity: int | None = None):
+        """Host trace with packed access traces: returns hits, offsets (n + 1
+        entries) and the packed visit / treelet arrays (ray r's entries are
+        offsets[r]:offsets[r+1]).  Arrays of `capacity` entries are tried
+        first (16 per ray by default); if the traces do not fit, the call is
+        made again with arrays of the size the first call reported."""
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        n = len(rays)
+        fl = None if flags is None else np.ascontiguousarray(flags, np.uint32)
+        hits = np.zeros(n, HIT_DTYPE)
+        offsets = np.zeros(n + 1, np.uint64)
+        total = C.c_uint64(0)
+        cap = 16 * n if capacity is None else int(capacity)
+        for _ in range(2):
+            vis = np.zeros(max(cap, 1), np.uint32) if want_visits else None
+            tl = np.zeros(max(cap, 1), np.uint32) if want_treelets else None
+            st = lib().rt_trace_host_packed(self._h, rays.ctypes.data, ptr(fl), default_flags, n, mode, row_capacity,
+                                            hits.ctypes.data, offsets.ctypes.data, ptr(vis), ptr(tl), cap,
+                                            C.byref(total))
+            if st == RT_ERR_TOO_LARGE and total.value > cap:
+                cap = total.value
+                continue
+            check(st)
+            break
+        t = int(total.value)
+        return hits, offsets, None if vis is None else vis[:t], None if tl is None else tl[:t]
 
     def bounce(self, rays, hits, out, seed: int = 7, tmin: float = 1e-4, tmax: float = 1e30, stream: int = 0,
                n: int | None = None) -> None:

@@ -16,6 +16,7 @@ f32p = C.POINTER(C.c_float)
 vp = C.c_void_p
 
 RT_OK = 0
+RT_ERR_TOO_LARGE = 6
 STATUS_NAMES = {0: "RT_OK", 1: "RT_ERR_INVALID", 2: "RT_ERR_CUDA", 3: "RT_ERR_OOM", 4: "RT_ERR_BLOB",
                 5: "RT_ERR_STATE", 6: "RT_ERR_TOO_LARGE", 7: "RT_ERR_TIMEOUT", 8: "RT_ERR_NO_DEVICE"}
 
@@ -154,6 +155,8 @@ PROTOTYPES = {
     "rt_scene_pinned_info": (C.c_int, [vp, C.POINTER(PinnedInfo)]),
     "rt_scene_set_device_offset": (C.c_int, [vp, C.c_uint64]),
     "rt_trace_host_noalloc": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
+    "rt_trace_host_packed": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, vp, vp,
+                                       C.c_uint64, vp]),
     "rt_batch_create": (C.c_int, [vp, C.POINTER(vp), C.c_uint32, C.POINTER(vp)]),
     "rt_batch_destroy": (C.c_int, [vp]),
     "rt_batch_set_items": (C.c_int, [vp, vp, vp, C.c_uint32]),
