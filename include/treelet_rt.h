@@ -270,9 +270,11 @@ rt_status rt_trace_host(rt_scene* scene, const rt_ray* rays, const uint32_t* fla
  * not n x row_capacity.  `offsets` holds n + 1 entries; `capacity` is the
  * entries `visits` and `treelets` each hold.  *total receives the entries
  * written; when it exceeds `capacity`, hits, offsets and *total are still
- * filled, the arrays are left alone and the call returns RT_ERR_TOO_LARGE
- * (call again with arrays of *total entries).  n x row_capacity must stay
- * below 2^32 and n at most 2^24.  Synchronous. */
+ * filled, the arrays' contents are unspecified and the call returns
+ * RT_ERR_TOO_LARGE (call again with arrays of *total entries).  Calls of
+ * 2^19 rays or more run as chunks whose packing and copies overlap the next
+ * chunk's trace (page-locked arrays let the copies run at full speed).
+ * n x row_capacity must stay below 2^32 and n at most 2^24.  Synchronous. */
 rt_status rt_trace_host_packed(rt_scene* scene, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags,
                                uint32_t n, uint32_t mode, uint32_t row_capacity, rt_hit* hits, uint64_t* offsets,
                                uint32_t* visits, uint32_t* treelets, uint64_t capacity, uint64_t* total);

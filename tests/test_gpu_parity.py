@@ -132,13 +132,54 @@ def test_hand_derived_edge_cases(ctx):
         scene.close()
 
 
-def test_trace_overflow_truncates(ctx):
+@pytest.mark.parametrize("cap", [6, 8, 16])
+def test_trace_overflow_truncates(ctx, cap):
+    """Rows shorter than the traces: capacities that are not a multiple of 8
+    are written entry by entry, multiples of 8 a 32-byte sector at a time
+    through shared memory; both keep each ray's first `cap` entries."""
     import treelet_rt as rt
 
     blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 4096, 9)
     rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 32, 32, 1, 0, 1e-4, 1e30)
-    oh = _check_all_modes(ctx, blob, rays, cap=6)
+    oh = _check_all_modes(ctx, blob, rays, cap=cap)
     assert (oh["status"] & rt.RAY_TRACE_OVERFLOW).any()
+
+
+def test_unaligned_trace_rows(ctx):
+    """Device rows that do not start on a 32-byte boundary (an offset of one
+    entry into the caller's buffer) take the entry-by-entry stores; rows that
+    do take the staged sector writes: both equal the oracle."""
+    import torch
+
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 8192, 10)
+    prim = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 40, 40, 1, 2, 1e-4, 1e30)
+    ph, _, _ = orc.trace(blob.bytes(), prim, 0, threads=8)
+    rays = np.concatenate([prim, rt.bounce_rays_host(blob, prim, ph, seed=8)])
+    n, cap = len(rays), 64
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    tl = orc.Treelets(blob.bytes(), 8192)
+    d_rays = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8).copy()).cuda()
+    for mode, omode, name in _modes():
+        oh, ov, ot = orc.trace(blob.bytes(), rays, omode, tl, capacity=cap, want_visits=True, want_treelets=True,
+                               threads=8)
+        for shift in (0, 1):
+            d_hits = torch.zeros(n * 64, dtype=torch.uint8, device="cuda")
+            vb = torch.zeros(n * cap + 8, dtype=torch.int32, device="cuda")
+            tb = torch.zeros(n * cap + 8, dtype=torch.int32, device="cuda")
+            d_vis, d_tl = vb[shift:shift + n * cap], tb[shift:shift + n * cap]
+            scene.trace(d_rays, d_hits, mode, visits=d_vis, treelets=d_tl, capacity=cap, n=n)
+            torch.cuda.synchronize()
+            hits = np.frombuffer(d_hits.cpu().numpy().tobytes(), rt.HIT_DTYPE)
+            assert_hits_equal(hits, oh, f"{name} hits, row shift {shift}")
+            assert_traces_equal(d_vis.cpu().numpy().view(np.uint32).reshape(n, cap), ov, oh["n_visits"],
+                                f"{name} visits, row shift {shift}")
+            assert_traces_equal(d_tl.cpu().numpy().view(np.uint32).reshape(n, cap), ot, oh["n_visits"],
+                                f"{name} treelet ids, row shift {shift}")
+    scene.close()
 
 
 @pytest.mark.parametrize("tuning", [dict(staged_slots=1, staged_epoch=1, staged_min_votes=1),
@@ -448,5 +489,53 @@ def test_packed_host_traces_match_oracle(ctx, cap):
                                        rt.MODE_TREELET, cap, h.ctypes.data, o.ctypes.data, v.ctypes.data, None,
                                        total - 1, C.byref(got))
     assert st == rt.RT_ERR_TOO_LARGE and got.value == total == int(o[-1])
-    assert not v.any()
+    assert_hits_equal(h, oh, "hits of a call whose traces did not fit")
+    scene.close()
+
+
+@pytest.mark.parametrize("mapped", [False, True])
+def test_packed_host_traces_chunked(ctx, mapped):
+    """A call of 2^20 rays runs as four chunks whose packing and copies
+    overlap the next chunk's trace, into pageable or page-locked output
+    arrays.  Hits and packed traces must equal rt_trace_host's rows cut to
+    each ray's length, and the counters one launch's."""
+    import torch
+
+    import treelet_rt as rt
+
+    blob = rt.Blob.gen(rt.SCENE_TERRAIN_INSTANCES, 2 * 256 * 256, 3)
+    n = 1 << 20
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_TERRAIN_INSTANCES), 1024, 1024, 1, 6, 1e-4, 1e30)[:n]
+    cap = 24
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    for mode, _, name in _modes():
+        hits, vis, tids = scene.trace_host(rays, mode, capacity=cap, want_visits=True, want_treelets=True)
+        ref_stats = scene.stats()
+        keep = np.minimum(hits["n_visits"], cap).astype(np.int64)
+        mask = np.arange(cap)[None, :] < keep[:, None]
+        total = int(keep.sum())
+        if mapped:
+            t_off = torch.zeros((n + 1) * 8, dtype=torch.uint8).pin_memory()
+            t_vis = torch.zeros(total * 4, dtype=torch.uint8).pin_memory()
+            t_tl = torch.zeros(total * 4, dtype=torch.uint8).pin_memory()
+            h = np.zeros(n, rt.HIT_DTYPE)
+            import ctypes as C
+
+            got = C.c_uint64(0)
+            rt.check(rt.lib().rt_trace_host_packed(scene.handle, rays.ctypes.data, None, rt.RAY_FLAG_OPAQUE, n, mode,
+                                                   cap, h.ctypes.data, t_off.data_ptr(), t_vis.data_ptr(),
+                                                   t_tl.data_ptr(), total, C.byref(got)))
+            off = t_off.numpy().view(np.uint64)
+            pv, pt = t_vis.numpy().view(np.uint32), t_tl.numpy().view(np.uint32)
+            assert got.value == total
+        else:
+            h, off, pv, pt = scene.trace_host_packed(rays, mode, row_capacity=cap, want_visits=True,
+                                                     want_treelets=True, capacity=total)
+        assert h.tobytes() == hits.tobytes(), f"{name}: packed-call hits differ"
+        assert off[0] == 0 and (np.diff(off.astype(np.int64)) == keep).all(), name
+        assert np.array_equal(pv, vis[mask]), f"{name} packed visits"
+        assert np.array_equal(pt, tids[mask]), f"{name} packed treelet ids"
+        st = scene.stats()
+        assert st["node_bytes"] == ref_stats["node_bytes"] and st["device_status"] == 0, name
     scene.close()

@@ -146,6 +146,7 @@ struct rt_scene {
   size_t io_bytes = 0;
   void* d_pack = nullptr;  // packed access traces of rt_trace_host_packed
   size_t pack_bytes = 0;
+  unsigned long long* h_tot = nullptr;  // page-locked chunk totals of rt_trace_host_packed
   rti::QueueScratch qs;  // treelet queues of RT_MODE_STAGED with queue_rounds
 };
 
@@ -360,6 +361,7 @@ rt_status launch_queued(rtk::TraceArgs& a, const rt_tuning& t, uint32_t largest_
   const uint32_t n_blocks = (n_bins + rtk::kBinScanItems - 1) / rtk::kBinScanItems;
   if (n_blocks > rtk::kBinScanItems)
     return rti::fail(RT_ERR_TOO_LARGE, "treelet queues: more than 2^24 treelets");
+  a.tbuf_off = rtk::kNone;  // rays move between lanes: trace entries go straight to the rows
   RT_CUDA(cudaMemsetAsync(qs.ctr, 0, sizeof(uint32_t) * 2 * (rti::kMaxQueueRounds + 1), st));
   RT_CUDA(cudaMemsetAsync(qs.hist, 0, sizeof(uint32_t) * n_bins, st));
   const uint32_t bt = rtk::kStagedMaxThreads;
@@ -424,14 +426,27 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
     RT_CUDA(cudaMemsetAsync(a.status, 0, sizeof(uint32_t), st));
   }
   RT_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), st));
-  if (mode == RT_MODE_PLAIN) {
+  // A launch that writes traces runs the walks compiled with the trace code
+  // (TRACED); they write the rows a whole 32-byte sector at a time through
+  // shared memory (rtk::trace_put) when every row starts on a 32-byte
+  // boundary, else entry by entry.
+  const bool traced = a.cap != 0;
+  const bool stage_rows = traced && (a.cap % 8u) == 0 && ((uintptr_t)a.visits & 31u) == 0 &&
+                          ((uintptr_t)a.tl_trace & 31u) == 0;
+  a.tbuf_off = rtk::kNone;
+  if (mode == RT_MODE_PLAIN || mode == RT_MODE_TREELET) {
     const uint32_t bt = t.block_threads;
-    auto kern = a.n_items ? rtk::trace_plain_kernel<CAP, true> : rtk::trace_plain_kernel<CAP, false>;
-    kern<<<persistent_grid((const void*)kern, bt, a.n), bt, 0, st>>>(a);
-  } else if (mode == RT_MODE_TREELET) {
-    const uint32_t bt = t.block_threads;
-    auto kern = a.n_items ? rtk::trace_treelet_kernel<CAP, true> : rtk::trace_treelet_kernel<CAP, false>;
-    kern<<<persistent_grid((const void*)kern, bt, a.n), bt, 0, st>>>(a);
+    const size_t dyn = stage_rows ? (size_t)(bt / 32) * rtk::kTraceBufWarpBytes + 128 : 0;
+    if (stage_rows) a.tbuf_off = 0;
+    void (*kern)(rtk::TraceArgs);
+    if (mode == RT_MODE_PLAIN)
+      kern = a.n_items ? (traced ? rtk::trace_plain_kernel<CAP, true, true> : rtk::trace_plain_kernel<CAP, true, false>)
+                       : (traced ? rtk::trace_plain_kernel<CAP, false, true> : rtk::trace_plain_kernel<CAP, false, false>);
+    else
+      kern = a.n_items
+                 ? (traced ? rtk::trace_treelet_kernel<CAP, true, true> : rtk::trace_treelet_kernel<CAP, true, false>)
+                 : (traced ? rtk::trace_treelet_kernel<CAP, false, true> : rtk::trace_treelet_kernel<CAP, false, false>);
+    kern<<<persistent_grid((const void*)kern, bt, a.n, dyn), bt, dyn, st>>>(a);
   } else if (qs) {
     if (a.n_items) return rti::fail(RT_ERR_INVALID, "staged traces run over one scene");
     return launch_queued<CAP>(a, t, largest_image, *qs, st);
@@ -450,12 +465,18 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
       a.pin_bytes = 0;
       a.pin_root = 0;
     }
-    while (slots > 0 && (uint64_t)a.pin_bytes + (uint64_t)warps * slots * slot_bytes + 128 > limit) --slots;
+    const uint64_t tbuf = stage_rows ? (uint64_t)warps * rtk::kTraceBufWarpBytes + 128 : 0;
+    while (slots > 0 && (uint64_t)a.pin_bytes + (uint64_t)warps * slots * slot_bytes + tbuf + 128 > limit) --slots;
     a.slots = slots;
     a.slot_bytes = slot_bytes;
     a.min_votes = t.staged_min_votes;
-    const size_t dyn = (size_t)a.pin_bytes + (size_t)warps * slots * slot_bytes + 128;
-    auto kern = slots ? rtk::trace_staged_kernel<CAP, true> : rtk::trace_staged_kernel<CAP, false>;
+    size_t dyn = (size_t)a.pin_bytes + (size_t)warps * slots * slot_bytes + 128;
+    if (stage_rows) {  // after the pinned image and the slots, on a 128-byte boundary
+      a.tbuf_off = (uint32_t)((dyn - 128 + 127) & ~(size_t)127);
+      dyn = a.tbuf_off + (size_t)warps * rtk::kTraceBufWarpBytes + 128;
+    }
+    auto kern = slots ? (traced ? rtk::trace_staged_kernel<CAP, true, true> : rtk::trace_staged_kernel<CAP, true, false>)
+                      : (traced ? rtk::trace_staged_kernel<CAP, false, true> : rtk::trace_staged_kernel<CAP, false, false>);
     RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     kern<<<persistent_grid((const void*)kern, bt, a.n, dyn), bt, dyn, st>>>(a);
   }
@@ -600,6 +621,7 @@ rt_status rt_scene_destroy(rt_scene* s) {
   cudaFree(s->d_queue);
   cudaFree(s->d_io);
   cudaFree(s->d_pack);
+  if (s->h_tot) cudaFreeHost(s->h_tot);
   cudaFree(s->qs.base);
   for (uint32_t c = 0; c < rti::kHostChunks; ++c) {
     if (s->ev_in[c]) cudaEventDestroy(s->ev_in[c]);
@@ -1405,36 +1427,47 @@ __global__ void trace_counts_kernel(const rt_hit* __restrict__ hits, uint32_t n,
   if (r < n) counts[r] = min(hits[r].n_visits, cap);
 }
 
-// offsets[r] = the totals of the scan blocks before r's + r's offset within
-// its block; offsets[n] = the total.
-__global__ void trace_offsets_kernel(const uint32_t* __restrict__ local, const uint32_t* __restrict__ block_sum,
+// Turns the block-local exclusive offsets of bin_scan_kernel into offsets
+// within the chunk (in place) and writes the chunk's total.
+__global__ void trace_offsets_kernel(uint32_t* __restrict__ off, const uint32_t* __restrict__ block_sum,
                                      const rt_hit* __restrict__ hits, uint32_t n, uint32_t cap,
-                                     unsigned long long* __restrict__ offsets) {
+                                     unsigned long long* __restrict__ total) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < n) offsets[r] = (unsigned long long)block_sum[r / rtk::kBinScanItems] + local[r];
-  if (r == n - 1)
-    offsets[n] = (unsigned long long)block_sum[r / rtk::kBinScanItems] + local[r] + min(hits[r].n_visits, cap);
+  if (r >= n) return;
+  const uint32_t o = block_sum[r / rtk::kBinScanItems] + off[r];
+  off[r] = o;
+  if (r == n - 1) *total = (unsigned long long)o + min(hits[r].n_visits, cap);
 }
 
-// One warp per ray copies the used prefix of its trace rows to its place in
-// the packed arrays.
+// One warp per ray: the ray's global offset (base + chunk offset) into
+// `goff`, and the used prefix of its trace rows to its place in the packed
+// arrays (NULL: not written).  Destinations may be device memory or mapped,
+// page-locked host memory.
 __global__ void trace_pack_kernel(const uint32_t* __restrict__ vis_rows, const uint32_t* __restrict__ tl_rows,
-                                  const unsigned long long* __restrict__ offsets, uint32_t n, uint32_t cap,
+                                  const uint32_t* __restrict__ off, uint32_t n, uint32_t cap, uint32_t chunk_total,
+                                  unsigned long long base, unsigned long long* __restrict__ goff,
                                   uint32_t* __restrict__ vis, uint32_t* __restrict__ tl) {
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t r = warp; r < n; r += warps) {
-    const unsigned long long o = offsets[r];
-    const uint32_t m = (uint32_t)(offsets[r + 1] - o);
+    const uint32_t o = off[r];
+    const uint32_t m = (r + 1 < n ? off[r + 1] : chunk_total) - o;
+    if (lane == 0) goff[r] = base + o;
+    const uint64_t row = (uint64_t)r * cap;
     for (uint32_t j = lane; j < m; j += 32) {
-      if (vis_rows) vis[o + j] = vis_rows[(uint64_t)r * cap + j];
-      if (tl_rows) tl[o + j] = tl_rows[(uint64_t)r * cap + j];
+      if (vis) vis[o + j] = vis_rows[row + j];
+      if (tl) tl[o + j] = tl_rows[row + j];
     }
   }
 }
 
 }  // namespace
 
+// Chunks pipeline the call: rays of every chunk go in on one stream; chunk c
+// is traced, counted and scanned on one of two streams while the host waits
+// for chunk c-1's total, then packs chunk c-1 into a device staging area and
+// copies it out on a third, so that copies and packing overlap the next
+// chunk's trace.
 extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const uint32_t* flags,
                                           uint32_t default_flags, uint32_t n, uint32_t mode, uint32_t row_capacity,
                                           rt_hit* hits, uint64_t* offsets, uint32_t* visits, uint32_t* treelets,
@@ -1458,14 +1491,21 @@ extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const
   rt_status st = check_trace(s, mode, &probe, "rt_trace_host_packed");
   if (st != RT_OK) return st;
   RT_CUDA(cudaSetDevice(s->ctx->device));
+  const uint32_t cap = row_capacity;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  const uint32_t n_blocks = (n + rtk::kBinScanItems - 1) / rtk::kBinScanItems;
+  uint64_t bound[rti::kHostChunks + 1];
+  uint32_t chunks = 1;
+  bound[0] = 0;
+  bound[1] = n;
+  if (!queued(s, mode)) chunks = rti::host_chunk_bounds(n, bound);
   const size_t b_rays = al(sizeof(rt_ray) * (size_t)n), b_flags = flags ? al(sizeof(uint32_t) * (size_t)n) : 0;
-  const size_t b_hits = al(sizeof(rt_hit) * (size_t)n), b_row = al(sizeof(uint32_t) * (size_t)n * row_capacity);
-  const size_t b_cnt = al(sizeof(uint32_t) * (size_t)n), b_blk = al(sizeof(uint32_t) * rtk::kBinScanItems);
-  const size_t b_off = al(sizeof(unsigned long long) * ((size_t)n + 1));
-  const size_t need =
-      b_rays + b_flags + b_hits + (visits ? b_row : 0) + (treelets ? b_row : 0) + 2 * b_cnt + b_blk + b_off;
+  const size_t b_hits = al(sizeof(rt_hit) * (size_t)n), b_row = al(sizeof(uint32_t) * (size_t)n * cap);
+  const size_t b_cnt = al(sizeof(uint32_t) * (size_t)n);
+  const size_t b_blk = al(sizeof(uint32_t) * rtk::kBinScanItems) * rti::kHostChunks;
+  const size_t b_goff = al(sizeof(unsigned long long) * (size_t)n);
+  const size_t b_tot = al(sizeof(unsigned long long) * rti::kHostChunks);
+  const size_t need = b_rays + b_flags + b_hits + (visits ? b_row : 0) + (treelets ? b_row : 0) + 2 * b_cnt + b_blk +
+                      b_goff + b_tot;
   if (need > s->io_bytes) {
     cudaFree(s->d_io);
     s->d_io = nullptr;
@@ -1473,6 +1513,13 @@ extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const
     st = dalloc((uint8_t**)&s->d_io, need);
     if (st != RT_OK) return st;
     s->io_bytes = need;
+  }
+  if (!s->h_tot) {
+    cudaError_t e = cudaHostAlloc(&s->h_tot, sizeof(unsigned long long) * rti::kHostChunks, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      s->h_tot = nullptr;
+      return cuda_fail(e, "rt_trace_host_packed: cudaHostAlloc");
+    }
   }
   uint8_t* p = (uint8_t*)s->d_io;
   auto take = [&](size_t b) {
@@ -1486,60 +1533,96 @@ extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const
   uint32_t* d_vis = visits ? (uint32_t*)take(b_row) : nullptr;
   uint32_t* d_tl = treelets ? (uint32_t*)take(b_row) : nullptr;
   uint32_t* d_cnt = (uint32_t*)take(b_cnt);
-  uint32_t* d_loc = (uint32_t*)take(b_cnt);
+  uint32_t* d_off = (uint32_t*)take(b_cnt);
   uint32_t* d_blk = (uint32_t*)take(b_blk);
-  unsigned long long* d_off = (unsigned long long*)take(b_off);
-  cudaStream_t cs = s->stream;
-  cudaError_t e = cudaMemcpyAsync(d_rays, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, cs);
-  if (e == cudaSuccess && flags)
-    e = cudaMemcpyAsync(d_flags, flags, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, cs);
-  if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
-  rt_trace_buf rows{d_vis, d_tl, row_capacity};
-  st = trace_launch(s, d_rays, d_flags, default_flags, n, mode, d_hits, &rows, cs, s->d_queue, false);
-  if (st != RT_OK) return host_finish(s, st);
-  trace_counts_kernel<<<(n + 255) / 256, 256, 0, cs>>>(d_hits, n, row_capacity, d_cnt);
-  rtk::bin_scan_kernel<<<n_blocks, 1024, 0, cs>>>(d_cnt, d_loc, d_blk, n);
-  rtk::bin_scan_top_kernel<<<1, 1024, 0, cs>>>(d_blk, n_blocks);
-  trace_offsets_kernel<<<(n + 255) / 256, 256, 0, cs>>>(d_loc, d_blk, d_hits, n, row_capacity, d_off);
-  e = cudaGetLastError();
-  unsigned long long tot = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&tot, d_off + n, sizeof(tot), cudaMemcpyDeviceToHost, cs);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
-  if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
-  *total = tot;
-  e = cudaMemcpyAsync(hits, d_hits, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, cs);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(offsets, d_off, sizeof(unsigned long long) * ((size_t)n + 1), cudaMemcpyDeviceToHost, cs);
-  if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
-  if (tot > capacity) {
-    st = host_finish(s, RT_OK);
-    if (st != RT_OK) return st;
-    return rti::fail(RT_ERR_TOO_LARGE, "rt_trace_host_packed: " + std::to_string(tot) +
-                                           " trace entries exceed the arrays' capacity (hits and offsets are filled)");
-  }
-  const size_t b_pack = al(sizeof(uint32_t) * (size_t)tot);
-  const size_t pack_need = (visits ? b_pack : 0) + (treelets ? b_pack : 0) + 256;
-  if (pack_need > s->pack_bytes) {
-    e = cudaStreamSynchronize(cs);
-    if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
-    cudaFree(s->d_pack);
-    s->d_pack = nullptr;
-    s->pack_bytes = 0;
-    st = dalloc((uint8_t**)&s->d_pack, pack_need);
-    if (st != RT_OK) return host_finish(s, st);
-    s->pack_bytes = pack_need;
-  }
-  uint32_t* p_vis = visits ? (uint32_t*)s->d_pack : nullptr;
-  uint32_t* p_tl = treelets ? (uint32_t*)((uint8_t*)s->d_pack + (visits ? b_pack : 0)) : nullptr;
-  if (tot > 0) {
-    trace_pack_kernel<<<std::min<uint32_t>((n + 7) / 8, 152 * 16), 256, 0, cs>>>(d_vis, d_tl, d_off, n, row_capacity,
-                                                                                  p_vis, p_tl);
+  unsigned long long* d_goff = (unsigned long long*)take(b_goff);
+  unsigned long long* d_tot = (unsigned long long*)take(b_tot);
+  const size_t blk_stride = al(sizeof(uint32_t) * rtk::kBinScanItems) / sizeof(uint32_t);
+
+  RT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, s->xin));
+  RT_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->xin));
+  cudaError_t e = cudaSuccess;
+  // every chunk's rays in, trace, counts, offsets and total
+  for (uint32_t c = 0; c < chunks && e == cudaSuccess && st == RT_OK; ++c) {
+    const size_t lo = bound[c];
+    const uint32_t m = (uint32_t)(bound[c + 1] - bound[c]);
+    e = cudaMemcpyAsync(d_rays + lo, rays + lo, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, s->xin);
+    if (e == cudaSuccess && flags)
+      e = cudaMemcpyAsync(d_flags + lo, flags + lo, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, s->xin);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev_in[c], s->xin);
+    cudaStream_t cs = (c & 1) ? s->stream2 : s->stream;
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, s->ev_in[c], 0);
+    if (e != cudaSuccess) break;
+    rt_trace_buf rows{d_vis ? d_vis + lo * cap : nullptr, d_tl ? d_tl + lo * cap : nullptr, cap};
+    st = trace_launch(s, d_rays + lo, d_flags ? d_flags + lo : nullptr, default_flags, m, mode, d_hits + lo, &rows, cs,
+                      s->d_queue + c, true);
+    if (st != RT_OK) break;
+    const uint32_t nb = (m + rtk::kBinScanItems - 1) / rtk::kBinScanItems;
+    uint32_t* blk = d_blk + c * blk_stride;
+    trace_counts_kernel<<<(m + 255) / 256, 256, 0, cs>>>(d_hits + lo, m, cap, d_cnt + lo);
+    rtk::bin_scan_kernel<<<nb, 1024, 0, cs>>>(d_cnt + lo, d_off + lo, blk, m);
+    rtk::bin_scan_top_kernel<<<1, 1024, 0, cs>>>(blk, nb);
+    trace_offsets_kernel<<<(m + 255) / 256, 256, 0, cs>>>(d_off + lo, blk, d_hits + lo, m, cap, d_tot + c);
     e = cudaGetLastError();
-    if (e == cudaSuccess && visits)
-      e = cudaMemcpyAsync(visits, p_vis, sizeof(uint32_t) * (size_t)tot, cudaMemcpyDeviceToHost, cs);
-    if (e == cudaSuccess && treelets)
-      e = cudaMemcpyAsync(treelets, p_tl, sizeof(uint32_t) * (size_t)tot, cudaMemcpyDeviceToHost, cs);
-    if (e != cudaSuccess) return host_finish(s, cuda_fail(e, "rt_trace_host_packed"));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->h_tot + c, d_tot + c, sizeof(unsigned long long), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev_done[c], cs);
   }
-  return host_finish(s, RT_OK);
+  // in chunk order: the chunk's total, then its packing and copies
+  unsigned long long base = 0;
+  bool fits = true;
+  for (uint32_t c = 0; c < chunks && e == cudaSuccess && st == RT_OK; ++c) {
+    const size_t lo = bound[c];
+    const uint32_t m = (uint32_t)(bound[c + 1] - bound[c]);
+    e = cudaEventSynchronize(s->ev_done[c]);
+    if (e != cudaSuccess) break;
+    const unsigned long long tot_c = reinterpret_cast<volatile unsigned long long*>(s->h_tot)[c];
+    fits = fits && base + tot_c <= capacity;
+    uint32_t *dst_vis = nullptr, *dst_tl = nullptr;
+    if (fits && tot_c > 0) {
+      // one staging area for the packed entries of one chunk: the pack and
+      // copy of chunk c follow chunk c-1's on the same stream
+      const size_t b_pack = al(sizeof(uint32_t) * (size_t)tot_c);
+      const size_t pack_need = (visits ? b_pack : 0) + (treelets ? b_pack : 0);
+      if (pack_need > s->pack_bytes) {
+        e = cudaStreamSynchronize(s->xout);
+        if (e != cudaSuccess) break;
+        cudaFree(s->d_pack);
+        s->d_pack = nullptr;
+        s->pack_bytes = 0;
+        st = dalloc((uint8_t**)&s->d_pack, pack_need + pack_need / 4);
+        if (st != RT_OK) break;
+        s->pack_bytes = pack_need + pack_need / 4;
+      }
+      dst_vis = visits ? (uint32_t*)s->d_pack : nullptr;
+      dst_tl = treelets ? (uint32_t*)((uint8_t*)s->d_pack + (visits ? b_pack : 0)) : nullptr;
+    }
+    e = cudaStreamWaitEvent(s->xout, s->ev_done[c], 0);
+    if (e != cudaSuccess) break;
+    unsigned long long* goff = d_goff + lo;
+    // 128-thread blocks, few registers: they fit beside the persistent trace
+    // of the next chunk on an SM instead of waiting for it to end
+    trace_pack_kernel<<<std::min<uint32_t>((m + 3) / 4, 152 * 8), 128, 0, s->xout>>>(
+        d_vis ? d_vis + lo * cap : nullptr, d_tl ? d_tl + lo * cap : nullptr, d_off + lo, m, cap, (uint32_t)tot_c, base,
+        goff, dst_vis, dst_tl);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hits + lo, d_hits + lo, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, s->xout);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(offsets + lo, d_goff + lo, sizeof(unsigned long long) * m, cudaMemcpyDeviceToHost, s->xout);
+    if (dst_vis && e == cudaSuccess)
+      e = cudaMemcpyAsync(visits + base, dst_vis, sizeof(uint32_t) * tot_c, cudaMemcpyDeviceToHost, s->xout);
+    if (dst_tl && e == cudaSuccess)
+      e = cudaMemcpyAsync(treelets + base, dst_tl, sizeof(uint32_t) * tot_c, cudaMemcpyDeviceToHost, s->xout);
+    base += tot_c;
+  }
+  if (st == RT_OK && e != cudaSuccess) st = cuda_fail(e, "rt_trace_host_packed");
+  st = host_finish(s, st);
+  if (st != RT_OK) return st;
+  offsets[n] = base;
+  *total = base;
+  if (base > capacity)
+    return rti::fail(RT_ERR_TOO_LARGE, "rt_trace_host_packed: " + std::to_string(base) +
+                                           " trace entries exceed the arrays' capacity (hits and offsets are filled)");
+  return RT_OK;
 }

@@ -278,17 +278,20 @@ void refresh_bf16(rt_mlp* m) {
                                                                           m->W3P);
 }
 
-// Column splits of the row-tile passes of the output layer: about two CTAs
-// per SM over the row tiles of the batch.
+// Column splits of the row-tile passes of the output layer: two waves of
+// two CTAs per SM over the row tiles of the batch (at most 152 splits: the
+// partial-result buffer holds 2 x 152 per row).
 uint32_t out_splits(const rt_mlp* m, uint32_t n) {
   const uint32_t tiles = (n + tcm::TM - 1) / tcm::TM, chunks = m->Cp / tcm::TN;
-  const uint32_t want = (2 * 152 + tiles - 1) / tiles;
-  return std::max<uint32_t>(1, std::min(chunks, want));
+  const uint32_t want = (4 * 152 + tiles - 1) / tiles;
+  return std::max<uint32_t>(1, std::min(std::min(chunks, want), 152u));
 }
 
-constexpr size_t kSmemStats = 16384 + 65536 + 2048;
-constexpr size_t kSmemDh2 = 16384 + 32768 + 65536 + 32768 + 1024;
-constexpr size_t kSmemDw3 = 32768 + 16384 + 65536 + 20480 + 1024;
+// Shared memory per CTA.  Pass 1 needs 49 KiB but asks for 80, so that
+// exactly two CTAs share an SM (and its 512 TMEM columns).
+constexpr size_t kSmemStats = 80 * 1024;
+constexpr size_t kSmemDh2 = 16384 + 16384 + 32768 + 16384 + 512;
+constexpr size_t kSmemDw3 = 16384 + 16384 + 32768 + 20480 + 512;
 
 tcm::OutArgs out_args(rt_mlp* m, const rt_mlp_sample* s, uint32_t n) {
   tcm::OutArgs a{};
@@ -318,12 +321,12 @@ void output_forward(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, uint32_t* top
   const tcm::OutArgs a = out_args(m, s, n);
   const dim3 grid((n + tcm::TM - 1) / tcm::TM, a.splits);
   if (top4) {
-    tcm::out_stats_kernel<true><<<grid, 128, kSmemStats, m->st>>>(a);
-    tcm::out_top4_kernel<<<blocks(n), 256, 0, m->st>>>(m->part, a.splits, n, top4);
+    tcm::out_stats_kernel<true><<<grid, tcm::kThreads, kSmemStats, m->st>>>(a);
+    tcm::out_top4_kernel<<<blocks(n), 256, 0, m->st>>>(m->part, 2 * a.splits, n, top4);
     return;
   }
-  tcm::out_stats_kernel<false><<<grid, 128, kSmemStats, m->st>>>(a);
-  tcm::out_lse_kernel<<<blocks(n), 256, 0, m->st>>>(m->part, a.splits, n, s, m->C, m->lse, m->loss);
+  tcm::out_stats_kernel<false><<<grid, tcm::kThreads, kSmemStats, m->st>>>(a);
+  tcm::out_lse_kernel<<<blocks(n), 256, 0, m->st>>>(m->part, 2 * a.splits, n, s, m->C, m->lse, m->loss);
 }
 
 // Gradients of the output layer: dW3, db3 into G, dH2 (zeroed first).
@@ -331,8 +334,8 @@ void output_backward(rt_mlp* m, const rt_mlp_sample* s, uint32_t n) {
   const tcm::OutArgs a = out_args(m, s, n);
   tcm::h2x_kernel<<<blocks((uint64_t)tcm::HX * RT_MLP_MAX_BATCH), 256, 0, m->st>>>(m->H2, n, RT_MLP_MAX_BATCH,
                                                                                    m->H2X);
-  tcm::out_dh2_kernel<<<dim3((n + tcm::TM - 1) / tcm::TM, a.splits), 128, kSmemDh2, m->st>>>(a);
-  tcm::out_dw3_kernel<<<m->Cp / tcm::TN, 128, kSmemDw3, m->st>>>(a);
+  tcm::out_dh2_kernel<<<dim3((n + tcm::TM - 1) / tcm::TM, a.splits), tcm::kThreads, kSmemDh2, m->st>>>(a);
+  tcm::out_dw3_kernel<<<m->Cp / tcm::TN, tcm::kThreads, kSmemDw3, m->st>>>(a);
 }
 
 int ksplit(int K, int tiles) {
@@ -434,7 +437,7 @@ rt_status rt_mlp_create(rt_ctx* ctx, uint32_t n_treelets, uint64_t seed, rt_mlp*
   chk(mk(&m->Z1, MB * H));
   chk(mk(&m->Z2, MB * H));
   chk(mk(&m->lse, MB));
-  chk(mk(&m->part, 8 * 152 * 2 * MB));  // the largest split count times 8 floats per row
+  chk(mk(&m->part, 8 * 152 * 2 * MB));  // 2 x 152 partial results of 8 floats per row
   chk(mk(&m->tstatus, 1));
   chk(mk(&m->dH2, MB * H));
   chk(mk(&m->dH1, MB * H));

@@ -32,10 +32,24 @@ namespace tcm {
 using bf16 = __nv_bfloat16;
 
 constexpr int TM = 128;          // rows of a tile (TMEM lanes)
-constexpr int TN = 256;          // columns (treelets) of a chunk
+constexpr int TN = 128;          // columns (treelets) of a chunk
 constexpr int HK = 64;           // hidden width (K of the logits product)
 constexpr int HX = 80;           // [h2 | 1 | 0 ...] rows of the dW3 operand
+// Eight warps a CTA: warp w reads TMEM lanes 32 (w % 4) .. 32 (w % 4) + 31
+// (the lanes a warp may access) and column half w / 4 of every chunk.
+constexpr int kThreads = 256;
+// TMEM columns a CTA allocates: two CTAs share an SM's 512, so one CTA's
+// epilogue runs while the other's MMAs and copies do.
+constexpr uint32_t kTmemCols = 256;
 constexpr uint32_t kTries = 1u << 22;
+constexpr float kLog2e = 1.4426950408889634f;
+
+// 2^x (MUFU ex2, flush-to-zero): the softmax exponentials in base 2.
+__device__ __forceinline__ float ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -86,13 +100,14 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 512 TMEM columns for the CTA (one warp allocates); returns the base address.
+// kTmemCols TMEM columns for the CTA (one warp allocates); returns the base address.
 // The .sync.aligned tcgen05 instructions need their whole warp converged,
 // hence the __syncwarp before each.
 __device__ __forceinline__ uint32_t tmem_alloc(uint32_t* slot, int warp) {
   __syncwarp();
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(su32(slot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(slot)),
+                 "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_before_sync();
@@ -105,7 +120,7 @@ __device__ __forceinline__ void tmem_free(uint32_t base, int warp) {
   tc_before_sync();
   __syncthreads();
   __syncwarp();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(base));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "n"(kTmemCols));
 }
 
 // 32 consecutive FP32 columns of this thread's TMEM lane; every lane of the
@@ -134,6 +149,9 @@ __device__ __forceinline__ uint32_t koff(uint32_t r, uint32_t k, uint32_t kx) {
 // Asynchronous 16-byte copy global -> shared (cp.async, L2 only).
 __device__ __forceinline__ void cp16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(su32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(su32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
@@ -177,7 +195,7 @@ __device__ __forceinline__ void split_range(const OutArgs& a, uint32_t sp, uint3
   c_end = min(chunks, c_beg + per);
 }
 
-// Logits of one chunk: D[128 x 256] = A[128 x 64] . B[256 x 64]^T, issued by one thread.
+// Logits of one chunk: D[128 x 128] = A[128 x 64] . B[128 x 64]^T, issued by one thread.
 __device__ __forceinline__ void mma_logits(uint32_t d, const uint8_t* a_tile, const uint8_t* b_tile) {
 #pragma unroll
   for (int kk = 0; kk < HK / 16; ++kk)
@@ -185,17 +203,53 @@ __device__ __forceinline__ void mma_logits(uint32_t d, const uint8_t* a_tile, co
         kk > 0 ? 1u : 0u);
 }
 
+// The chunk's biases into shared memory (asynchronously; zero past C).
+__device__ __forceinline__ void load_bias(float* dst, const float* b3, uint32_t c, uint32_t C) {
+  for (uint32_t j = threadIdx.x; j < (uint32_t)TN; j += blockDim.x) {
+    const uint32_t col = c * TN + j;
+    if (col < C) cp4(dst + j, b3 + col);
+    else dst[j] = 0.0f;
+  }
+}
+
+// 32 logits of this thread's row, bias added; columns past C and invalid
+// rows read -inf.
+__device__ __forceinline__ void logits32(uint32_t taddr, const float* bias, uint32_t col0, uint32_t C, bool valid_row,
+                                         float* v) {
+  tmem_ld32(taddr, v);
+  if (valid_row && col0 + 32 <= C) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] += bias[j];
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = (valid_row && col0 + j < C) ? v[j] + bias[j] : -INFINITY;
+  }
+}
+
+__device__ __forceinline__ float max32(const float* v) {
+  float t[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) t[j] = fmaxf(v[j], v[j + 16]);
+#pragma unroll
+  for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+    for (int j = 0; j < w; ++j) t[j] = fmaxf(t[j], t[j + w]);
+  return t[0];
+}
+
 // Pass 1: per row, the running maximum and exp-sum over the split's columns
 // and the target's logit (TOPK = false); or the four largest logits (TOPK).
+// Each thread covers one row and one column half of every chunk, so a row's
+// results are written as two partial results (index 2 * split + half).
 template <bool TOPK>
-__global__ void __launch_bounds__(128) out_stats_kernel(OutArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) out_stats_kernel(OutArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* a_tile = smem;                  // 128 x 64 bf16: 16 KiB
-  uint8_t* b_tile0 = smem + 16384;         // 256 x 64 bf16: 32 KiB, two buffers
-  float* bias = reinterpret_cast<float*>(smem + 16384 + 65536);  // 2 x 256
+  uint8_t* a_tile = smem;                                        // 128 x 64 bf16: 16 KiB
+  uint8_t* b_tile0 = smem + 16384;                               // 128 x 64 bf16: 16 KiB, two buffers
+  float* bias = reinterpret_cast<float*>(smem + 16384 + 32768);  // 2 x 128
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ uint32_t tmem_slot;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, half = warp >> 2;
   const uint32_t row0 = blockIdx.x * TM;
   uint32_t c_beg, c_end;
   split_range(a, blockIdx.y, c_beg, c_end);
@@ -204,7 +258,8 @@ __global__ void __launch_bounds__(128) out_stats_kernel(OutArgs a) {
     bar_init(&bars[1]);
   }
   const uint32_t tmem = tmem_alloc(&tmem_slot, warp);
-  const uint32_t row = row0 + tid;
+  const uint32_t lanes = tmem + ((uint32_t)(quad * 32) << 16);
+  const uint32_t row = row0 + (uint32_t)(quad * 32) + (uint32_t)(tid & 31);
   const bool valid_row = row < a.n;
   const uint32_t tgt = valid_row ? a.s[row].target : 0xFFFFFFFFu;
   float m = -INFINITY, ssum = 0.0f, zt = -INFINITY;
@@ -213,11 +268,8 @@ __global__ void __launch_bounds__(128) out_stats_kernel(OutArgs a) {
   uint32_t phase[2] = {0, 0};
   bool ok = true;
   auto load_chunk = [&](uint32_t c, int buf) {
-    load_tile(b_tile0 + buf * 32768, a.w3t, HK, c * TN, TN, a.cp, 0, HK);
-    for (uint32_t j = tid; j < TN; j += blockDim.x) {
-      const uint32_t col = c * TN + j;
-      bias[buf * TN + j] = col < a.C ? a.b3[col] : 0.0f;
-    }
+    load_tile(b_tile0 + buf * 16384, a.w3t, HK, c * TN, TN, a.cp, 0, HK);
+    load_bias(bias + buf * TN, a.b3, c, a.C);
   };
   if (c_beg < c_end) {
     load_tile(a_tile, a.h2, HK, row0, TM, a.n, 0, HK);
@@ -251,23 +303,16 @@ __global__ void __launch_bounds__(128) out_stats_kernel(OutArgs a) {
     __syncthreads();  // the next operand is in place, every thread saw chunk c's MMA complete
     if (c + 1 < c_end && tid == 0) {
       tc_after_sync();
-      mma_logits(tmem + (uint32_t)((buf ^ 1) * TN), a_tile, b_tile0 + (buf ^ 1) * 32768);
+      mma_logits(tmem + (uint32_t)((buf ^ 1) * TN), a_tile, b_tile0 + (buf ^ 1) * 16384);
       commit(&bars[buf ^ 1]);
     }
     // epilogue of chunk c, overlapping the next chunk's MMA
 #pragma unroll 1
-    for (int sl = 0; sl < TN / 32; ++sl) {
+    for (int sl = 0; sl < 2; ++sl) {
+      const uint32_t cl0 = (uint32_t)(half * 64 + sl * 32);  // column within the chunk
+      const uint32_t col0 = c * TN + cl0;
       float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * TN + sl * 32), v);
-      const uint32_t col0 = c * TN + sl * 32;
-      float mx = -INFINITY;
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const bool live = valid_row && col0 + j < a.C;
-        v[j] = live ? v[j] + bias[buf * TN + sl * 32 + j] : -INFINITY;
-        mx = fmaxf(mx, v[j]);
-        if (!TOPK && col0 + j == tgt) zt = v[j];
-      }
+      logits32(lanes + (uint32_t)(buf * TN) + cl0, bias + buf * TN + cl0, col0, a.C, valid_row, v);
       if (TOPK) {
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -292,13 +337,24 @@ __global__ void __launch_bounds__(128) out_stats_kernel(OutArgs a) {
             }
           }
         }
-      } else if (mx > -INFINITY) {
-        const float mn = fmaxf(m, mx);
-        float acc = ssum * __expf(m - mn);
+      } else {
+        if (tgt - col0 < 32u) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) acc += __expf(v[j] - mn);
-        ssum = acc;
-        m = mn;
+          for (int j = 0; j < 32; ++j)
+            if (col0 + j == tgt) zt = v[j];
+        }
+        const float mx = max32(v);
+        if (mx > -INFINITY) {
+          const float mn = fmaxf(m, mx), sh = mn * kLog2e;
+          float acc0 = ssum * ex2(fmaf(m, kLog2e, -sh)), acc1 = 0.0f;
+#pragma unroll
+          for (int j = 0; j < 32; j += 2) {
+            acc0 += ex2(fmaf(v[j], kLog2e, -sh));
+            acc1 += ex2(fmaf(v[j + 1], kLog2e, -sh));
+          }
+          ssum = acc0 + acc1;
+          m = mn;
+        }
       }
     }
     tc_before_sync();
@@ -306,24 +362,25 @@ __global__ void __launch_bounds__(128) out_stats_kernel(OutArgs a) {
   }
   if (!ok) atomicOr(a.status, 1u);
   cp_wait_all();  // no copy may still be landing when the CTA exits
+  const uint32_t splits2 = a.splits * 2, sp = blockIdx.y * 2 + (uint32_t)half;
   if (valid_row) {
     if (TOPK) {
-      float* p = a.part + ((uint64_t)blockIdx.y * a.n + row) * 8;
+      float* p = a.part + ((uint64_t)sp * a.n + row) * 8;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         p[2 * k] = tv[k];
         p[2 * k + 1] = __uint_as_float(ti[k]);
       }
     } else {
-      a.part[((uint64_t)0 * a.splits + blockIdx.y) * a.n + row] = m;
-      a.part[((uint64_t)1 * a.splits + blockIdx.y) * a.n + row] = ssum;
-      a.part[((uint64_t)2 * a.splits + blockIdx.y) * a.n + row] = zt;
+      a.part[((uint64_t)0 * splits2 + sp) * a.n + row] = m;
+      a.part[((uint64_t)1 * splits2 + sp) * a.n + row] = ssum;
+      a.part[((uint64_t)2 * splits2 + sp) * a.n + row] = zt;
     }
   }
   tmem_free(tmem, warp);
 }
 
-// Pass 1 combined over the splits: lse per row and the mean loss.
+// Pass 1 combined over the partial results: lse per row and the mean loss.
 __global__ void out_lse_kernel(const float* __restrict__ part, uint32_t splits, uint32_t n, const rt_mlp_sample* s,
                                uint32_t C, float* __restrict__ lse, float* __restrict__ loss) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -343,7 +400,7 @@ __global__ void out_lse_kernel(const float* __restrict__ part, uint32_t splits, 
   if (s[b].target < C) atomicAdd(loss, (l - zt) / (float)n);
 }
 
-// Pass 1 (TOPK) combined: the four largest over the splits' candidates.
+// Pass 1 (TOPK) combined: the four largest over the partial results' candidates.
 __global__ void out_top4_kernel(const float* __restrict__ part, uint32_t splits, uint32_t n, uint32_t* __restrict__ out) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n) return;
@@ -366,33 +423,34 @@ __global__ void out_top4_kernel(const float* __restrict__ part, uint32_t splits,
   for (int q = 0; q < 4; ++q) out[(uint64_t)b * 4 + q] = ti[q];
 }
 
-// dz of element (row, col) from its logit z (bias included).
-__device__ __forceinline__ float dz_of(float z, float lse, uint32_t col, uint32_t tgt, float inv_n, bool live) {
-  const float p = __expf(z - lse);
-  return live ? (p - (col == tgt ? 1.0f : 0.0f)) * inv_n : 0.0f;
+// dz of element (row, col) from its logit z (bias included, -inf where not
+// live): (softmax - onehot) / n, with sh = lse * log2(e).
+__device__ __forceinline__ float dz_of(float z, float sh, uint32_t col, uint32_t tgt, float inv_n) {
+  return (ex2(fmaf(z, kLog2e, -sh)) - (col == tgt ? 1.0f : 0.0f)) * inv_n;
 }
 
 // Pass 2: dh2[tile] += dz[tile, split's columns] . W3^T.
-__global__ void __launch_bounds__(128) out_dh2_kernel(OutArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) out_dh2_kernel(OutArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* a_tile = smem;                   // h2 tile: 16 KiB
-  uint8_t* bz = smem + 16384;               // W3^T chunk: 32 KiB
-  uint8_t* dz = smem + 16384 + 32768;       // dz tile 128 x 256 (K-major, K = 256): 64 KiB
-  uint8_t* bw = smem + 16384 + 32768 + 65536;  // W3 tile 64 x 256 (K-major): 32 KiB
-  float* bias = reinterpret_cast<float*>(smem + 16384 + 32768 + 65536 + 32768);
+  uint8_t* a_tile = smem;                     // h2 tile 128 x 64: 16 KiB
+  uint8_t* bz = smem + 16384;                 // W3^T chunk 128 x 64: 16 KiB
+  uint8_t* dz = smem + 32768;                 // dz tile 128 x 128 (K-major, K = 128): 32 KiB
+  uint8_t* bw = smem + 65536;                 // W3 tile 64 x 128 (K-major, K = 128): 16 KiB
+  float* bias = reinterpret_cast<float*>(smem + 81920);
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, half = warp >> 2;
   const uint32_t row0 = blockIdx.x * TM;
   uint32_t c_beg, c_end;
   split_range(a, blockIdx.y, c_beg, c_end);
   if (tid == 0) bar_init(&bar);
   const uint32_t tmem = tmem_alloc(&tmem_slot, warp);
+  const uint32_t lanes = tmem + ((uint32_t)(quad * 32) << 16);
   const uint32_t d_h = tmem + TN;  // dh2 accumulator: 64 columns after the logits
-  const uint32_t row = row0 + tid;
+  const uint32_t r = (uint32_t)(quad * 32) + (uint32_t)(tid & 31), row = row0 + r;
   const bool valid_row = row < a.n;
   const uint32_t tgt = valid_row ? a.s[row].target : 0xFFFFFFFFu;
-  const float l = valid_row ? a.lse[row] : 0.0f;
+  const float sh = valid_row ? a.lse[row] * kLog2e : 0.0f;
   const float inv_n = 1.0f / (float)a.n;
   uint32_t phase = 0;
   bool ok = true;
@@ -400,7 +458,7 @@ __global__ void __launch_bounds__(128) out_dh2_kernel(OutArgs a) {
   for (uint32_t c = c_beg; c < c_end; ++c) {
     load_tile(bz, a.w3t, HK, c * TN, TN, a.cp, 0, HK);
     load_tile(bw, a.w3p, a.cp, 0, HK, HK, c * TN, TN);
-    for (uint32_t j = tid; j < TN; j += blockDim.x) bias[j] = c * TN + j < a.C ? a.b3[c * TN + j] : 0.0f;
+    load_bias(bias, a.b3, c, a.C);
     cp_commit();
     cp_wait_all();
     fence_async_smem();
@@ -415,24 +473,23 @@ __global__ void __launch_bounds__(128) out_dh2_kernel(OutArgs a) {
     phase ^= 1u;
     tc_after_sync();
 #pragma unroll 1
-    for (int sl = 0; sl < TN / 32; ++sl) {
+    for (int sl = 0; sl < 2; ++sl) {
+      const uint32_t cl0 = (uint32_t)(half * 64 + sl * 32);
+      const uint32_t col0 = c * TN + cl0;
       float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(sl * 32), v);
-      const uint32_t col0 = c * TN + sl * 32;
+      logits32(lanes + cl0, bias + cl0, col0, a.C, valid_row, v);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         uint32_t w[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int j = q * 8 + 2 * e;
-          const float d0 = dz_of(v[j] + bias[sl * 32 + j], l, col0 + j, tgt, inv_n, valid_row && col0 + j < a.C);
-          const float d1 =
-              dz_of(v[j + 1] + bias[sl * 32 + j + 1], l, col0 + j + 1, tgt, inv_n, valid_row && col0 + j + 1 < a.C);
+          const float d0 = dz_of(v[j], sh, col0 + j, tgt, inv_n);  // ex2(-inf) = 0: dead columns give 0
+          const float d1 = dz_of(v[j + 1], sh, col0 + j + 1, tgt, inv_n);
           const __nv_bfloat162 pr = __floats2bfloat162_rn(d0, d1);
           w[e] = *reinterpret_cast<const uint32_t*>(&pr);
         }
-        *reinterpret_cast<uint4*>(dz + koff((uint32_t)tid, (uint32_t)(sl * 32 + q * 8), TN)) =
-            make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4*>(dz + koff(r, cl0 + (uint32_t)(q * 8), TN)) = make_uint4(w[0], w[1], w[2], w[3]);
       }
     }
     fence_async_smem();
@@ -453,45 +510,46 @@ __global__ void __launch_bounds__(128) out_dh2_kernel(OutArgs a) {
   if (!ok) atomicOr(a.status, 1u);
   cp_wait_all();  // no copy may still be landing when the CTA exits
   if (c_beg < c_end) {
-    // tcgen05.ld is warp-collective: every lane loads, valid rows store
+    // tcgen05.ld is warp-collective: every lane loads, valid rows store; the
+    // two column halves of the CTA take 32 of the 64 columns each
     float v[32];
-    for (int h = 0; h < HK; h += 32) {
-      tmem_ld32(d_h + ((uint32_t)(warp * 32) << 16) + (uint32_t)h, v);
-      if (valid_row) {
+    tmem_ld32(d_h + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * 32), v);
+    if (valid_row) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) atomicAdd(a.dh2 + (uint64_t)row * HK + h + j, v[j]);
-      }
+      for (int j = 0; j < 32; ++j) atomicAdd(a.dh2 + (uint64_t)row * HK + half * 32 + j, v[j]);
     }
   }
   tmem_free(tmem, warp);
 }
 
-// Pass 3: per 256-column chunk, [dW3 | db3]^T = sum over row tiles of dz^T . [h2 | 1].
-__global__ void __launch_bounds__(128) out_dw3_kernel(OutArgs a) {
+// Pass 3: per 128-column chunk, [dW3 | db3]^T = sum over row tiles of dz^T . [h2 | 1].
+__global__ void __launch_bounds__(kThreads, 2) out_dw3_kernel(OutArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* bz = smem;                         // W3^T chunk: 32 KiB (the CTA's, fixed)
-  uint8_t* a_tile = smem + 32768;             // h2 tile: 16 KiB
-  uint8_t* dzt = smem + 32768 + 16384;        // dz^T: two 128 x 128 halves (K-major, K = 128): 64 KiB
-  uint8_t* bx = smem + 32768 + 16384 + 65536; // [h2 | 1]^T tile 80 x 128 (K-major): 20 KiB
-  float* bias = reinterpret_cast<float*>(smem + 32768 + 16384 + 65536 + 20480);
+  uint8_t* bz = smem;                          // W3^T chunk 128 x 64: 16 KiB (the CTA's, fixed)
+  uint8_t* a_tile = smem + 16384;              // h2 tile 128 x 64: 16 KiB
+  uint8_t* dzt = smem + 32768;                 // dz^T 128 x 128 (K-major, K = 128 rows): 32 KiB
+  uint8_t* bx = smem + 65536;                  // [h2 | 1]^T tile 80 x 128 (K-major): 20 KiB
+  float* bias = reinterpret_cast<float*>(smem + 65536 + 20480);
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, half = warp >> 2;
   const uint32_t c = blockIdx.x;  // chunk
   if (tid == 0) bar_init(&bar);
   const uint32_t tmem = tmem_alloc(&tmem_slot, warp);
-  const uint32_t d_w0 = tmem + TN, d_w1 = tmem + TN + HX;  // the two halves' accumulators (80 columns each)
+  const uint32_t lanes = tmem + ((uint32_t)(quad * 32) << 16);
+  const uint32_t d_w = tmem + TN;  // [dW3 | db3]^T accumulator: 80 columns after the logits
   const float inv_n = 1.0f / (float)a.n;
   const uint32_t tiles = (a.n + TM - 1) / TM;
+  const uint32_t r = (uint32_t)(quad * 32) + (uint32_t)(tid & 31);
   uint32_t phase = 0;
   bool ok = true;
   load_tile(bz, a.w3t, HK, c * TN, TN, a.cp, 0, HK);
-  for (uint32_t j = tid; j < TN; j += blockDim.x) bias[j] = c * TN + j < a.C ? a.b3[c * TN + j] : 0.0f;
+  load_bias(bias, a.b3, c, a.C);
   for (uint32_t t = 0; t < tiles; ++t) {
-    const uint32_t row0 = t * TM, row = row0 + tid;
+    const uint32_t row0 = t * TM, row = row0 + r;
     const bool valid_row = row < a.n;
     const uint32_t tgt = valid_row ? a.s[row].target : 0xFFFFFFFFu;
-    const float l = valid_row ? a.lse[row] : 0.0f;
+    const float sh = valid_row ? a.lse[row] * kLog2e : 0.0f;
     load_tile(a_tile, a.h2, HK, row0, TM, a.n, 0, HK);
     load_tile(bx, a.h2x, a.ldx, 0, HX, HX, row0, TM);
     cp_commit();
@@ -508,17 +566,16 @@ __global__ void __launch_bounds__(128) out_dw3_kernel(OutArgs a) {
     phase ^= 1u;
     tc_after_sync();
 #pragma unroll 1
-    for (int sl = 0; sl < TN / 32; ++sl) {
+    for (int sl = 0; sl < 2; ++sl) {
+      const uint32_t cl0 = (uint32_t)(half * 64 + sl * 32);
+      const uint32_t col0 = c * TN + cl0;
       float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(sl * 32), v);
-      const uint32_t col0 = c * TN + sl * 32;
+      logits32(lanes + cl0, bias + cl0, col0, a.C, valid_row, v);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const uint32_t cl = (uint32_t)(sl * 32 + j);  // column within the chunk
-        const float d = dz_of(v[j] + bias[cl], l, col0 + j, tgt, inv_n, valid_row && col0 + j < a.C);
-        // dz^T: element (column cl, row tid) of half cl / 128
-        *reinterpret_cast<bf16*>(dzt + (cl >> 7) * 32768u + koff(cl & 127u, (uint32_t)tid, TM)) =
-            __float2bfloat16_rn(d);
+        // dz^T: element (column cl0 + j, row r)
+        *reinterpret_cast<bf16*>(dzt + koff(cl0 + (uint32_t)j, r, TM)) =
+            __float2bfloat16_rn(dz_of(v[j], sh, col0 + j, tgt, inv_n));
       }
     }
     fence_async_smem();
@@ -527,11 +584,9 @@ __global__ void __launch_bounds__(128) out_dw3_kernel(OutArgs a) {
     if (tid == 0) {
       tc_after_sync();
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
-#pragma unroll
-        for (int kk = 0; kk < TM / 16; ++kk)
-          mma(h ? d_w1 : d_w0, sdesc(su32(dzt) + h * 32768u + kk * 256u, TM * 16u), sdesc(su32(bx) + kk * 256u, TM * 16u),
-              idesc(TM, HX), (t > 0 || kk > 0) ? 1u : 0u);
+      for (int kk = 0; kk < TM / 16; ++kk)
+        mma(d_w, sdesc(su32(dzt) + kk * 256u, TM * 16u), sdesc(su32(bx) + kk * 256u, TM * 16u), idesc(TM, HX),
+            (t > 0 || kk > 0) ? 1u : 0u);
       commit(&bar);
     }
     if (!bar_wait(&bar, phase)) ok = false;
@@ -539,21 +594,20 @@ __global__ void __launch_bounds__(128) out_dw3_kernel(OutArgs a) {
     tc_after_sync();
   }
   if (!ok) atomicOr(a.status, 1u);
-  // lane tid of each half is column c * 256 + half * 128 + tid: 64 weight
-  // gradients, then the bias gradient
-  for (int h = 0; h < 2; ++h) {
-    const uint32_t col = c * TN + (uint32_t)h * TM + (uint32_t)tid;
-    const uint32_t base = (h ? d_w1 : d_w0) + ((uint32_t)(warp * 32) << 16);
-    float v[32];
-    for (int q = 0; q < 3; ++q) {  // columns 0..95 of the 80: the last load reads past 80, within the allocation
-      tmem_ld32(base + (uint32_t)(q * 32), v);
-      if (col < a.C) {
+  cp_wait_all();
+  // lane r of the accumulator is column c * 128 + r: 64 weight gradients,
+  // then the bias gradient; column half 0 takes k 0..31, half 1 k 32..95
+  // (the last load reads past the 80 columns, within the allocation)
+  const uint32_t col = c * TN + r;
+  float v[32];
+  for (int q = half; q < (half ? 3 : 1); ++q) {
+    tmem_ld32(d_w + ((uint32_t)(quad * 32) << 16) + (uint32_t)(q * 32), v);
+    if (col < a.C) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int k = q * 32 + j;
-          if (k < HK) a.dw3[(uint64_t)k * a.C + col] = v[j];
-          else if (k == HK) a.db3[col] = v[j];
-        }
+      for (int j = 0; j < 32; ++j) {
+        const int k = q * 32 + j;
+        if (k < HK) a.dw3[(uint64_t)k * a.C + col] = v[j];
+        else if (k == HK) a.db3[col] = v[j];
       }
     }
   }

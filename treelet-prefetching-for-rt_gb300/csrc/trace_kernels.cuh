@@ -76,7 +76,68 @@ struct TraceArgs {
   uint32_t min_votes;          // lanes that must want a treelet before a warp stages it
   const uint32_t* hint;        // staged: predicted next treelet per (treelet, direction octant), or null
   uint32_t wait_tries;         // staged: probes of the wait for the pinned image before staging stops
+  uint32_t tbuf_off;           // byte offset of the trace staging area in dynamic shared memory
+                               // (128-aligned base), kNone: trace entries go straight to the rows
 };
+
+// Trace staging (the plain walk).  A lane writing its ray's trace rows one
+// 4-byte entry at a time leaves partly written 32-byte sectors that L2 fills
+// from DRAM and writes back again and again (4.5x the entries' bytes
+// written, as many read, on bounce rays).  Instead each lane keeps its ray's
+// next 8 entries
+// of each row in its warp's 2 KiB staging area ([visit | treelet][entry
+// 0..7][lane] words: lanes hit distinct banks) and writes them as one whole,
+// aligned sector.  Used when the row capacity is a multiple of 8 and the rows
+// start on 32-byte boundaries; the last partial sector is written when the
+// ray ends.
+constexpr uint32_t kTraceBufWarpBytes = 2048;
+
+extern __shared__ __align__(128) uint8_t rt_dyn_smem[];
+
+// The calling lane's entry 0 of its warp's staging area.
+__device__ __forceinline__ uint32_t* trace_buf(uint32_t off) {
+  uint8_t* base = rt_dyn_smem + ((128u - ((uint32_t)__cvta_generic_to_shared(rt_dyn_smem) & 127u)) & 127u);
+  return reinterpret_cast<uint32_t*>(base + off + (threadIdx.x >> 5) * kTraceBufWarpBytes) + (threadIdx.x & 31u);
+}
+
+// Entry n (< capacity) of a ray's visit and treelet rows (either row may be null).
+__device__ __forceinline__ void trace_put(const TraceArgs& a, uint32_t* vrow, uint32_t* trow, uint32_t n, uint32_t vis,
+                                          uint32_t tl) {
+  if (a.tbuf_off == kNone) {
+    if (vrow) vrow[n] = vis;
+    if (trow) trow[n] = tl;
+    return;
+  }
+  uint32_t* b = trace_buf(a.tbuf_off);
+  const uint32_t j = n & 7u;
+  if (vrow) b[j * 32] = vis;
+  if (trow) b[256 + j * 32] = tl;
+  if (j == 7u) {
+    if (vrow) {
+      uint4* d = reinterpret_cast<uint4*>(vrow + (n - 7u));
+      __stcs(d, make_uint4(b[0], b[32], b[64], b[96]));
+      __stcs(d + 1, make_uint4(b[128], b[160], b[192], b[224]));
+    }
+    if (trow) {
+      uint4* d = reinterpret_cast<uint4*>(trow + (n - 7u));
+      __stcs(d, make_uint4(b[256], b[288], b[320], b[352]));
+      __stcs(d + 1, make_uint4(b[384], b[416], b[448], b[480]));
+    }
+  }
+}
+
+// Writes the staged entries of a ray's last partial sector; m = entries
+// recorded (at most the capacity).
+__device__ __forceinline__ void trace_drain(const TraceArgs& a, uint32_t* vrow, uint32_t* trow, uint32_t m) {
+  const uint32_t k = m & 7u;
+  if (a.tbuf_off == kNone || k == 0) return;
+  const uint32_t* b = trace_buf(a.tbuf_off);
+  const uint32_t base = m - k;
+  for (uint32_t j = 0; j < k; ++j) {
+    if (vrow) vrow[base + j] = b[j * 32];
+    if (trow) trow[base + j] = b[256 + j * 32];
+  }
+}
 
 struct Recorder {
   uint32_t* vrow;
@@ -85,11 +146,10 @@ struct Recorder {
   uint32_t n;
   uint32_t bytes;
   const uint2* meta;
-  __device__ __forceinline__ void rec(uint32_t unit, uint32_t type) {
-    if (n < cap) {
-      if (vrow) vrow[n] = rtf::pack_visit(unit, type);
-      if (trow) trow[n] = meta[unit].x;
-    }
+  // TRACED = false: a launch without traces, whose walk only counts.
+  template <bool TRACED>
+  __device__ __forceinline__ void rec(const TraceArgs& a, uint32_t unit, uint32_t type) {
+    if (TRACED && n < cap) trace_put(a, vrow, trow, n, rtf::pack_visit(unit, type), trow ? meta[unit].x : 0u);
     n++;
     bytes += rtf::tx_bytes(type);
   }
@@ -259,7 +319,9 @@ __device__ __forceinline__ void run_persistent(const TraceArgs& a, W& w, unsigne
 // the internal node descended next (the first hit internal child, :2570-2578);
 // leaves and further children are pushed.  A top-level instance leaf is
 // followed by its whole BLAS before the next top-level entry (:2602-2679).
-template <int CAP, bool MULTI>
+// TRACED = false compiles the walk of a launch without traces (no trace
+// code at all); TRACED = true writes the rows.
+template <int CAP, bool MULTI, bool TRACED>
 struct PlainWalker {
   rtm::V3 O, D, idir;
   float tmin, tmax, min_thit, c_tobj;
@@ -300,7 +362,7 @@ struct PlainWalker {
     ic_fast = false;
     idir = rtm::calculate_idir(D);
     fast = rtd::finite_ray(O, D, tmin, tmax);
-    rec.rec(0, rtf::TX_STRUCTURE);
+    rec.rec<TRACED>(a, 0, rtf::TX_STRUCTURE);
     const uint4 h0 = __ldg(v.blob), h1 = __ldg(v.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
@@ -316,7 +378,6 @@ struct PlainWalker {
   }
 
   __device__ __forceinline__ void visit_internal(const TraceArgs& a, uint32_t unit, const rtd::Node64& nd) {
-    rec.rec(unit, rtf::TX_INTERNAL);
     // one box test for both levels (the world ray, or the instance's object
     // ray with the culling distance scaled into object space): lanes at TLAS
     // and BLAS nodes run it together
@@ -345,8 +406,8 @@ struct PlainWalker {
     if (status & RT_RAY_STACK_OVERFLOW) stop(0);
   }
 
-  __device__ __forceinline__ void visit_leaf(const TraceArgs& a, uint32_t unit, const rtd::Node64& q) {
-    rec.rec(unit, rtf::TX_LEAF_DESC);
+  // Returns the transaction type of the leaf's second record.
+  __device__ __forceinline__ uint32_t visit_leaf(const TraceArgs& a, uint32_t unit, const rtd::Node64& q) {
     if (rtf::leaf_type_of(q.w[1]) == 0) {
       const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
       const rtm::V3 v1 = rtm::v3(__uint_as_float(q.w[7]), __uint_as_float(q.w[8]), __uint_as_float(q.w[9]));
@@ -359,24 +420,25 @@ struct PlainWalker {
         c_leaf = unit;
         c_inst = ic.unit;
         c_tobj = t;
-        rec.rec(unit, rtf::TX_QUAD_LEAF_HIT);
         if (terminate) sp = 0;
-      } else {
-        rec.rec(unit, rtf::TX_QUAD_LEAF);
+        return rtf::TX_QUAD_LEAF_HIT;
       }
-    } else {
-      status |= RT_RAY_HIT_PROCEDURAL;
-      rec.rec(unit, rtf::TX_PROCEDURAL_LEAF);
+      return rtf::TX_QUAD_LEAF;
     }
+    status |= RT_RAY_HIT_PROCEDURAL;
+    return rtf::TX_PROCEDURAL_LEAF;
   }
 
-  __device__ __forceinline__ void visit_instance(const TraceArgs& a, uint32_t unit, const rtd::Node64& q) {
-    rec.rec(unit, rtf::TX_INSTANCE_LEAF);
+  // Returns the unit of the instance's second record (its BLAS header), or
+  // kNone when the header lies outside the blob.
+  __device__ __forceinline__ uint32_t visit_instance(const TraceArgs& a, uint32_t unit, const rtd::Node64& q) {
     rtd::Instance in;
     rtd::instance_from(q, v.blob + (uint64_t)unit * 4, 0, in);
     const uint64_t hdr = (uint64_t)unit * 64 + in.bvh_address;
-    if ((hdr & 63) || hdr / 64 >= v.n_units) return stop(RT_RAY_BAD_NODE);
-    rec.rec((uint32_t)(hdr >> 6), rtf::TX_STRUCTURE);
+    if ((hdr & 63) || hdr / 64 >= v.n_units) {
+      stop(RT_RAY_BAD_NODE);
+      return kNone;
+    }
     const uint4 h0 = __ldg(v.blob + (hdr >> 4));
     const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
     enter_instance(in, unit, O, D, tmin, tmax, ic);
@@ -384,6 +446,7 @@ struct PlainWalker {
     push((uint32_t)(broot >> 6) << 2);
     inblas = true;
     if (status & RT_RAY_STACK_OVERFLOW) stop(0);
+    return (uint32_t)(hdr >> 6);
   }
 
   // One node visit (the caller checks active() first).  The node to visit is
@@ -424,24 +487,39 @@ struct PlainWalker {
     if (unit + (kind == 2 ? 1u : 0u) >= v.n_units) return stop(RT_RAY_BAD_NODE);
     rtd::Node64 q;
     rtd::load64(v.blob + (uint64_t)unit * 4, 0, q);
-    if (kind == 0) visit_internal(a, unit, q);
-    else if (kind == 1) visit_leaf(a, unit, q);
-    else visit_instance(a, unit, q);
+    // a visit records one or two transactions; two call sites for all kinds
+    // keep the recording code (staged through shared memory) out of every
+    // branch
+    rec.rec<TRACED>(a, unit, kind == 0 ? rtf::TX_INTERNAL : (kind == 1 ? rtf::TX_LEAF_DESC : rtf::TX_INSTANCE_LEAF));
+    uint32_t unit2 = unit, type2 = rtf::TX_STRUCTURE;
+    if (kind == 0) {
+      visit_internal(a, unit, q);
+      unit2 = kNone;
+    } else if (kind == 1) {
+      type2 = visit_leaf(a, unit, q);
+    } else {
+      unit2 = visit_instance(a, unit, q);
+    }
+    if (unit2 != kNone) rec.rec<TRACED>(a, unit2, type2);
   }
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
     const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);
+    if (TRACED) trace_drain(a, rec.vrow, rec.trow, min(rec.n, rec.cap));
     write_hit(a, v, r, !bad && (min_thit < tmax), min_thit, O, D, tmin, tmax, c_leaf, c_inst, c_tobj, rec, status);
   }
 };
 
 // The plain walk keeps its stack inside the walker, whose fields the compiler
-// then leaves in local memory: 48 registers and five 256-thread CTAs per SM.
+// then leaves in local memory: 48 registers and five 256-thread CTAs per SM
+// (the launch bound holds it there: with the trace staging the compiler
+// would take 54 registers and fit four CTAs, 2-8% slower untraced and 7%
+// slower traced on bounce rays).
 // Its fields in registers (90, or capped at 51-85 with spills) measured
 // 40-45% slower, while the treelet walks gained from them (below).
-template <int CAP, bool MULTI>
-__global__ void __launch_bounds__(256) trace_plain_kernel(TraceArgs a) {
-  PlainWalker<CAP, MULTI> w;
+template <int CAP, bool MULTI, bool TRACED>
+__global__ void __launch_bounds__(256, 5) trace_plain_kernel(TraceArgs a) {
+  PlainWalker<CAP, MULTI, TRACED> w;
   unsigned long long bytes = 0;
   run_persistent(a, w, bytes);
   if (a.stats) add_warp_total64(a.stats + ST_NODE_BYTES, bytes);

@@ -41,7 +41,9 @@ constexpr int kColdWords = 9;
 // stop between treelets and go on later in another thread: the treelet-queued
 // walk (trace_queued.cuh).  The local array then holds only the current
 // stack and the cold tail.
-template <int CAP, bool STAGED, bool MULTI, bool SLAB = false>
+// TRACED = false compiles the walk of a launch without traces (no trace code
+// at all).
+template <int CAP, bool STAGED, bool MULTI, bool SLAB = false, bool TRACED = true>
 struct Walker {
   static constexpr bool kColdWorld = !STAGED;
   static constexpr int kOtLocal = SLAB ? 0 : CAP;  // other-stack entries in the local array
@@ -115,12 +117,11 @@ struct Walker {
     return rtm::v3(hi(b), lo(c), hi(c));
   }
   // one visit of the trace (the reference's MemoryTransactionRecord)
-  __device__ __forceinline__ void record(uint32_t unit, uint32_t type) {
-    if (rec.n < rec.cap) {
+  __device__ __forceinline__ void record(const TraceArgs& a, uint32_t unit, uint32_t type) {
+    if (TRACED && rec.n < rec.cap) {
       uint32_t* vrow = reinterpret_cast<uint32_t*>(cold(4));
       uint32_t* trow = reinterpret_cast<uint32_t*>(cold(5));
-      if (vrow) vrow[rec.n] = rtf::pack_visit(unit, type);
-      if (trow) trow[rec.n] = v.meta[unit].x;
+      trace_put(a, vrow, trow, rec.n, rtf::pack_visit(unit, type), trow ? v.meta[unit].x : 0u);
     }
     rec.n++;
     rec.bytes += rtf::tx_bytes(type);
@@ -182,7 +183,7 @@ struct Walker {
     set_world(o, id);
     fast = rtd::finite_ray(o, D, tmin, tmax);
     ic_fast = false;
-    record(0, rtf::TX_STRUCTURE);
+    record(a, 0, rtf::TX_STRUCTURE);
     const uint4 h0 = __ldg(v.blob), h1 = __ldg(v.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
@@ -318,7 +319,7 @@ struct Walker {
       ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
     }
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
-      record(unit, rtf::TX_INTERNAL);
+      record(a, unit, rtf::TX_INTERNAL);
       uint32_t soff01 = 0, soff23 = 0, soff45 = 0;
       if (pinned) {  // route bits in bytes 16..17, child records in the tail
         const uint4 t = rtd::ld_shared_v4(saddr + rtp::IN_UNIT);
@@ -354,7 +355,7 @@ struct Walker {
         c += ci & 3u;
       }
     } else if (top) {  // instance leaf (:1870-1953)
-      record(unit, rtf::TX_INSTANCE_LEAF);
+      record(a, unit, rtf::TX_INSTANCE_LEAF);
       uint32_t hdr_unit, broot_unit, broot_soff = 0;
       if (pinned) {  // the 64-byte record: units, route bits, BLAS root record, rows
         hdr_unit = nd.w[rtp::IL_HDR_UNIT / 4];
@@ -370,11 +371,11 @@ struct Walker {
         const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
         broot_unit = (uint32_t)(broot >> 6);
       }
-      record(hdr_unit, rtf::TX_STRUCTURE);
+      record(a, hdr_unit, rtf::TX_STRUCTURE);
       const uint32_t cc = broot_soff ? ((broot_soff << kEShift) | kEPin) : (broot_unit << kEShift);
       push((rbits >> (kRouteInst + rsh)) & 1u, cc, unit);
     } else {  // primitive leaf (:2071-2196)
-      record(unit, rtf::TX_LEAF_DESC);
+      record(a, unit, rtf::TX_LEAF_DESC);
       const rtd::Node64& q = nd;
       if (rtf::leaf_type_of(q.w[1]) == 0) {
         const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
@@ -386,14 +387,14 @@ struct Walker {
         if (hit && tmin <= wt && wt <= tmax && wt < min_thit) {  // :2127-2141
           min_thit = t / ic.mult;
           set_hit(unit, inst, t);
-          record(unit, rtf::TX_QUAD_LEAF_HIT);
+          record(a, unit, rtf::TX_QUAD_LEAF_HIT);
           if (terminate) clear();
         } else {
-          record(unit, rtf::TX_QUAD_LEAF);
+          record(a, unit, rtf::TX_QUAD_LEAF);
         }
       } else {
         status |= RT_RAY_HIT_PROCEDURAL;
-        record(unit, rtf::TX_PROCEDURAL_LEAF);
+        record(a, unit, rtf::TX_PROCEDURAL_LEAF);
       }
     }
     if (status & RT_RAY_STACK_OVERFLOW) clear();
@@ -406,6 +407,8 @@ struct Walker {
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
     const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);
     const unsigned long long h = cold(2);
+    if (TRACED)
+      trace_drain(a, reinterpret_cast<uint32_t*>(cold(4)), reinterpret_cast<uint32_t*>(cold(5)), min(rec.n, rec.cap));
     const Recorder counts{nullptr, nullptr, rec.cap, rec.n, rec.bytes, v.meta};
     write_hit(a, v, r, !bad && (min_thit < tmax), min_thit, world_o(), dir(), tmin, tmax, (uint32_t)h,
               (uint32_t)(h >> 32), lo(cold(3)), counts, status);
@@ -418,10 +421,10 @@ struct Walker {
 // cold tail it fits four 256-thread CTAs per SM at 64 registers.
 constexpr int kTreeletMinBlocks = 4;
 
-template <int CAP, bool MULTI>
+template <int CAP, bool MULTI, bool TRACED>
 __global__ void __launch_bounds__(256, kTreeletMinBlocks) trace_treelet_kernel(TraceArgs a) {
   unsigned long long stack[2 * CAP + kColdWords];
-  Walker<CAP, false, MULTI> w;
+  Walker<CAP, false, MULTI, false, TRACED> w;
   w.stk = stack;
   w.pin_base = 0;
   w.pin_root = 0;
@@ -517,7 +520,7 @@ struct WarpStage {
 // reads that fall in a resident slot are served from shared memory.  A slot
 // is read only by its own warp; __syncwarp orders the slot's reads before it
 // is refilled.  SLOTS = false compiles the warp slots out (a.slots == 0).
-template <int CAP, bool SLOTS>
+template <int CAP, bool SLOTS, bool TRACED>
 __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_staged_kernel(TraceArgs a) {
   extern __shared__ __align__(128) uint8_t dyn_smem[];
   __shared__ WarpStage ws[kStagedMaxThreads / 32];
@@ -568,7 +571,7 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_sta
     return 0u;
   };
   unsigned long long stack[2 * CAP + kColdWords];
-  Walker<CAP, true, false> w;  // staged launches trace one scene
+  Walker<CAP, true, false, false, TRACED> w;  // staged launches trace one scene
   w.stk = stack;
   w.pin_base = pin_ok ? smem_u32(smem0) : 0u;
   w.pin_root = pin_ok ? a.pin_root : 0u;

@@ -228,9 +228,10 @@ def main():
     scene.bounce(d_r, d_h, d_ao, seed=201, tmin=1e-4, tmax=0.1, n=n_ao)
     del d_r, d_h, hp
     flags = rt.RAY_FLAG_TERMINATE_ON_FIRST_HIT | rt.RAY_FLAG_OPAQUE
-    for mode_name, mode in (("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
-        r = autotune(_FlagScene(scene, flags), d_ao, n_ao, mode, budgets=(4096, 8192, 16384, 32768), reps=args.reps,
-                     flush=flush)
+    scene.form_treelets(8192)
+    for mode_name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
+        budgets = None if mode == rt.MODE_PLAIN else (4096, 8192, 16384, 32768)
+        r = autotune(_FlagScene(scene, flags), d_ao, n_ao, mode, budgets=budgets, reps=args.reps, flush=flush)
         out["results"][f"{mode_name}/ao"] = r
         print(mode_name, "ao", r["budget"], r["tuning"], r["mrays_s"], flush=True)
     scene.close()
