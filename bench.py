@@ -57,7 +57,7 @@ def _peaks():
 # 262,144 rays per launch (the full launch of 2,097,152 rays is too large to capture with
 # --set full); scaled to a full launch by the ray count.
 STAGED_DRAM_BYTES_PER_RAY = {"primary": (103.862784e6 + 16.576000e6) / 262144,
-                             "bounce": (171.958528e6 + 33.870336e6) / 262144}
+                             "bounce": (172.382720e6 + 34.174464e6) / 262144}
 
 
 # What binds the staged walk, from the same ncu capture (bounce launch): it
@@ -65,8 +65,9 @@ STAGED_DRAM_BYTES_PER_RAY = {"primary": (103.862784e6 + 16.576000e6) / 262144,
 # divergence and issue instead.
 LIMITER = {"kind": "issue / SIMT divergence (dependent loads of a pointer-chasing walk), not HBM bandwidth",
            "source": "profiles/trace_kernels_terrain_instances.md, staged walk, 262,144 bounce rays",
-           "lanes_active_of_32": 9.37, "issue_slots_active_pct": 68.1, "warps_per_sm": 19.9,
-           "dram_busy_pct": 2.2, "l1_hit_pct": 55.1, "l2_hit_pct": 71.1}
+           "lanes_active_of_32": 8.93, "issue_slots_active_pct": 66.7, "warps_per_sm": 20.0,
+           "dram_busy_pct": 2.8, "l1_hit_pct": 54.8, "l2_hit_pct": 71.0, "l1_throughput_pct": 24.7,
+           "l2_throughput_pct": 12.8, "smem_pipe_pct": 1.9}
 
 
 def _traffic_per_ray():
@@ -662,12 +663,6 @@ def run_ao(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def _tuned_batch(mode_name: str) -> dict:
-    """The autotuned batch-launch tuning for a mode (plain / treelet), if any."""
-    r = _tuned(f"{mode_name}/batch")
-    return r["tuning"] if r else {}
-
-
 def run_batch(args) -> None:
     """256 scenes of log-uniform size (1K..1M triangles, unit-cube generator),
     each with a log-uniform ray batch (4K..256K rays, half primary, half
@@ -729,12 +724,13 @@ def run_batch(args) -> None:
             apply_tuning(s, name, "bounce")
             if name == "staged":
                 s.set_tuning(queue_rounds=rt.TUNING_OFF)
-        # the batch's own tuned entry, else the scenes' bounce tuning (the
-        # same stack depth as the per-scene launches it is compared with)
-        tuned = _tuned_batch(name) or apply_tuning(scenes[0], name, "bounce")
-        if tuned and name != "staged":
-            batch.set_tuning(**{k: v for k, v in tuned.items() if k in ("block_threads", "refill_lanes",
-                                                                         "stack_depth")})
+        # the batch launch's tile and queue parameters (CTA threads, refill
+        # lanes, stack depth) from the project's autotuner, run on this batch
+        tune = None
+        if name != "staged":
+            from treelet_rt.autotune import autotune_batch
+
+            tune = autotune_batch(batch, d_rays, n, mode, reps=2, passes=2, flush=flush)
 
         def per_scene():
             for i, s in enumerate(scenes):
@@ -751,6 +747,8 @@ def run_batch(args) -> None:
         out[name] = {"per_scene_launches_mrays_s": round(n / ms_scene / 1e3, 3),
                      "one_launch_mrays_s": round(n / ms_batch / 1e3, 3),
                      "graph_replay_mrays_s": round(n / ms_graph / 1e3, 3), "hits_equal": same}
+        if tune:
+            out[name]["autotuned"] = {"tuning": tune["tuning"], "candidates": tune["candidates"]}
     line = {"metric": "Mrays/s, 256 scenes in one persistent work-queue launch vs one launch per scene",
             "unit": "Mrays/s", "value": out["plain"]["graph_replay_mrays_s"], "higher_is_better": True, "n_gpus": 1,
             "config": {"workload": f"{n_scenes} scenes, triangles log-uniform 1K..1M (total {int(tris.sum())}), rays "

@@ -427,12 +427,13 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
   }
   RT_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), st));
   // A launch that writes traces runs the walks compiled with the trace code
-  // (TRACED); they write the rows a whole 32-byte sector at a time through
-  // shared memory (rtk::trace_put) when every row starts on a 32-byte
-  // boundary, else entry by entry.
+  // (TRACED).  The plain walk writes its rows a whole 32-byte sector at a
+  // time through shared memory (rtk::trace_put) when every row starts on a
+  // 32-byte boundary, else entry by entry; the treelet walks write entry by
+  // entry.
   const bool traced = a.cap != 0;
-  const bool stage_rows = traced && (a.cap % 8u) == 0 && ((uintptr_t)a.visits & 31u) == 0 &&
-                          ((uintptr_t)a.tl_trace & 31u) == 0;
+  const bool stage_rows = traced && mode == RT_MODE_PLAIN && (a.cap % 8u) == 0 &&
+                          ((uintptr_t)a.visits & 31u) == 0 && ((uintptr_t)a.tl_trace & 31u) == 0;
   a.tbuf_off = rtk::kNone;
   if (mode == RT_MODE_PLAIN || mode == RT_MODE_TREELET) {
     const uint32_t bt = t.block_threads;
@@ -465,16 +466,11 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
       a.pin_bytes = 0;
       a.pin_root = 0;
     }
-    const uint64_t tbuf = stage_rows ? (uint64_t)warps * rtk::kTraceBufWarpBytes + 128 : 0;
-    while (slots > 0 && (uint64_t)a.pin_bytes + (uint64_t)warps * slots * slot_bytes + tbuf + 128 > limit) --slots;
+    while (slots > 0 && (uint64_t)a.pin_bytes + (uint64_t)warps * slots * slot_bytes + 128 > limit) --slots;
     a.slots = slots;
     a.slot_bytes = slot_bytes;
     a.min_votes = t.staged_min_votes;
-    size_t dyn = (size_t)a.pin_bytes + (size_t)warps * slots * slot_bytes + 128;
-    if (stage_rows) {  // after the pinned image and the slots, on a 128-byte boundary
-      a.tbuf_off = (uint32_t)((dyn - 128 + 127) & ~(size_t)127);
-      dyn = a.tbuf_off + (size_t)warps * rtk::kTraceBufWarpBytes + 128;
-    }
+    const size_t dyn = (size_t)a.pin_bytes + (size_t)warps * slots * slot_bytes + 128;
     auto kern = slots ? (traced ? rtk::trace_staged_kernel<CAP, true, true> : rtk::trace_staged_kernel<CAP, true, false>)
                       : (traced ? rtk::trace_staged_kernel<CAP, false, true> : rtk::trace_staged_kernel<CAP, false, false>);
     RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));

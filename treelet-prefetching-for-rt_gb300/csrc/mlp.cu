@@ -168,13 +168,15 @@ __global__ void gelu_back(const float* __restrict__ dH, const float* __restrict_
   if (i < count) dZ[i] = __float2bfloat16(dH[i] * gelu_grad(Z[i]));
 }
 
-// out[c] = sum_r X[r][c]
+// out[c] += sum_r X[r][c]: one block per 128 rows, one thread per column
+// (out starts at zero).  One block over all rows took 0.22 ms for 4,096 x 64.
 __global__ void col_sum(const bf16* __restrict__ X, int rows, int cols, float* __restrict__ out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = threadIdx.x;
   if (c >= cols) return;
+  const int r0 = blockIdx.x * 128, r1 = min(rows, r0 + 128);
   float s = 0.0f;
-  for (int r = 0; r < rows; ++r) s += __bfloat162float(X[(size_t)r * cols + c]);
-  out[c] = s;
+  for (int r = r0; r < r1; ++r) s += __bfloat162float(X[(size_t)r * cols + c]);
+  atomicAdd(out + c, s);
 }
 
 __global__ void embed_grad(const float* __restrict__ dX, const rt_mlp_sample* __restrict__ s, int n, uint32_t C,
@@ -274,7 +276,7 @@ void refresh_bf16(rt_mlp* m) {
   to_bf16<<<blocks((uint64_t)m->C * EMB), 256, 0, m->st>>>(m->P, m->E16, (uint64_t)m->C * EMB);
   w1_to_bf16<<<blocks(XP * H), 256, 0, m->st>>>(m->P + m->offW1, m->W1_16);
   to_bf16<<<blocks(H * H), 256, 0, m->st>>>(m->P + m->offW2, m->W2_16, H * H);
-  tcm::w3_operands_kernel<<<blocks((uint64_t)H * m->Cp), 256, 0, m->st>>>(m->P + m->offW3, m->C, m->Cp, m->W3T,
+  tcm::w3_operands_kernel<<<m->Cp / 32, 256, 0, m->st>>>(m->P + m->offW3, m->C, m->Cp, m->W3T,
                                                                           m->W3P);
 }
 
@@ -291,7 +293,7 @@ uint32_t out_splits(const rt_mlp* m, uint32_t n) {
 // exactly two CTAs share an SM (and its 512 TMEM columns).
 constexpr size_t kSmemStats = 80 * 1024;
 constexpr size_t kSmemDh2 = 16384 + 16384 + 32768 + 16384 + 512;
-constexpr size_t kSmemDw3 = 16384 + 16384 + 32768 + 20480 + 512;
+constexpr size_t kSmemDw3 = 16384 + 16384 + tcm::kDztBytes + 20480 + 512;
 
 tcm::OutArgs out_args(rt_mlp* m, const rt_mlp_sample* s, uint32_t n) {
   tcm::OutArgs a{};
@@ -335,7 +337,9 @@ void output_backward(rt_mlp* m, const rt_mlp_sample* s, uint32_t n) {
   tcm::h2x_kernel<<<blocks((uint64_t)tcm::HX * RT_MLP_MAX_BATCH), 256, 0, m->st>>>(m->H2, n, RT_MLP_MAX_BATCH,
                                                                                    m->H2X);
   tcm::out_dh2_kernel<<<dim3((n + tcm::TM - 1) / tcm::TM, a.splits), tcm::kThreads, kSmemDh2, m->st>>>(a);
-  tcm::out_dw3_kernel<<<m->Cp / tcm::TN, tcm::kThreads, kSmemDw3, m->st>>>(a);
+  // two row halves per chunk, added into the zeroed gradient: 1,494 CTAs
+  // (4.9 waves of 304) instead of 747 (2.5 waves)
+  tcm::out_dw3_kernel<<<dim3(m->Cp / tcm::TN, 2), tcm::kThreads, kSmemDw3, m->st>>>(a);
 }
 
 int ksplit(int K, int tiles) {
@@ -366,7 +370,7 @@ rt_status run(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, bool grads, uint32_
   gelu_back<<<blocks((uint64_t)B * H), 256, 0, st>>>(m->dH2, m->Z2, m->dZ2, B * H);
   // W2, b2
   gemm<true, false, EPI_ACC>(H, H, B, m->H1, H, m->dZ2, H, m->G + m->offW2, H, nullptr, nullptr, ksplit(B, 1), st);
-  col_sum<<<1, H, 0, st>>>(m->dZ2, B, H, m->G + m->offb2);
+  col_sum<<<(B + 127) / 128, H, 0, st>>>(m->dZ2, B, H, m->G + m->offb2);
   // dH1 = dZ2 W2^T
   MLP_CUDA(cudaMemsetAsync(m->dH1, 0, sizeof(float) * B * H, st));
   gemm<false, true, EPI_ACC>(B, H, H, m->dZ2, H, m->W2_16, H, m->dH1, H, nullptr, nullptr, 1, st);
@@ -375,7 +379,7 @@ rt_status run(rt_mlp* m, const rt_mlp_sample* s, uint32_t n, bool grads, uint32_
   MLP_CUDA(cudaMemsetAsync(m->dW1, 0, sizeof(float) * XP * H, st));
   gemm<true, false, EPI_ACC>(XP, H, B, m->X, XP, m->dZ1, H, m->dW1, H, nullptr, nullptr, ksplit(B, 1), st);
   copy_rows<<<blocks(XIN * H), 256, 0, st>>>(m->dW1, H, m->G + m->offW1, XIN, H);
-  col_sum<<<1, H, 0, st>>>(m->dZ1, B, H, m->G + m->offb1);
+  col_sum<<<(B + 127) / 128, H, 0, st>>>(m->dZ1, B, H, m->G + m->offb1);
   // dX = dZ1 W1^T -> embedding rows
   MLP_CUDA(cudaMemsetAsync(m->dX, 0, sizeof(float) * B * XP, st));
   gemm<false, true, EPI_ACC>(B, XP, H, m->dZ1, H, m->W1_16, H, m->dX, XP, nullptr, nullptr, 1, st);

@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(kThreads, 2) out_stats_kernel(OutArgs a) {
   float m = -INFINITY, ssum = 0.0f, zt = -INFINITY;
   float tv[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
   uint32_t ti[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-  uint32_t phase[2] = {0, 0};
+  uint32_t phases = 0;  // bit b: the parity of buffer b's next phase
   bool ok = true;
   auto load_chunk = [&](uint32_t c, int buf) {
     load_tile(b_tile0 + buf * 16384, a.w3t, HK, c * TN, TN, a.cp, 0, HK);
@@ -292,8 +292,8 @@ __global__ void __launch_bounds__(kThreads, 2) out_stats_kernel(OutArgs a) {
       load_chunk(c + 1, buf ^ 1);
       cp_commit();
     }
-    if (!bar_wait(&bars[buf], phase[buf])) ok = false;
-    phase[buf] ^= 1u;
+    if (!bar_wait(&bars[buf], (phases >> buf) & 1u)) ok = false;
+    phases ^= 1u << buf;
     tc_after_sync();
     if (c + 1 < c_end) {
       cp_wait_all();
@@ -522,14 +522,32 @@ __global__ void __launch_bounds__(kThreads, 2) out_dh2_kernel(OutArgs a) {
   tmem_free(tmem, warp);
 }
 
-// Pass 3: per 128-column chunk, [dW3 | db3]^T = sum over row tiles of dz^T . [h2 | 1].
+// dz^T tile of pass 3 (128 treelet columns x 128 batch rows, K-major along
+// the rows) with its K-adjacent core matrices 144 bytes apart instead of
+// 128: a warp writes one column's 32 rows, and with 128-byte spacing rows r
+// and r + 8 fell on the same banks (40M conflicts of 65M shared-memory
+// wavefronts in pass 3); 144 bytes spreads the four groups of 8 rows over
+// 16 banks.
+constexpr uint32_t kDztLbo = 144, kDztSbo = 16 * kDztLbo;  // 16 K groups per 8-column group
+constexpr uint32_t kDztBytes = 16 * kDztSbo;               // 36 KiB
+__device__ __forceinline__ uint32_t dzt_off(uint32_t col, uint32_t row) {
+  return (col >> 3) * kDztSbo + (row >> 3) * kDztLbo + (col & 7u) * 16u + (row & 7u) * 2u;
+}
+__device__ __forceinline__ uint64_t sdesc_lbo(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Pass 3: per 128-column chunk and half of the row tiles (blockIdx.y),
+// [dW3 | db3]^T += sum over those row tiles of dz^T . [h2 | 1], added into
+// the zeroed gradient.
 __global__ void __launch_bounds__(kThreads, 2) out_dw3_kernel(OutArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* bz = smem;                          // W3^T chunk 128 x 64: 16 KiB (the CTA's, fixed)
   uint8_t* a_tile = smem + 16384;              // h2 tile 128 x 64: 16 KiB
-  uint8_t* dzt = smem + 32768;                 // dz^T 128 x 128 (K-major, K = 128 rows): 32 KiB
-  uint8_t* bx = smem + 65536;                  // [h2 | 1]^T tile 80 x 128 (K-major): 20 KiB
-  float* bias = reinterpret_cast<float*>(smem + 65536 + 20480);
+  uint8_t* dzt = smem + 32768;                 // dz^T 128 x 128 (K-major, K = 128 rows, padded): 36 KiB
+  uint8_t* bx = smem + 32768 + kDztBytes;      // [h2 | 1]^T tile 80 x 128 (K-major): 20 KiB
+  float* bias = reinterpret_cast<float*>(smem + 32768 + kDztBytes + 20480);
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, half = warp >> 2;
@@ -539,13 +557,14 @@ __global__ void __launch_bounds__(kThreads, 2) out_dw3_kernel(OutArgs a) {
   const uint32_t lanes = tmem + ((uint32_t)(quad * 32) << 16);
   const uint32_t d_w = tmem + TN;  // [dW3 | db3]^T accumulator: 80 columns after the logits
   const float inv_n = 1.0f / (float)a.n;
-  const uint32_t tiles = (a.n + TM - 1) / TM;
+  const uint32_t tiles = (a.n + TM - 1) / TM, per = (tiles + gridDim.y - 1) / gridDim.y;
+  const uint32_t t_beg = min(tiles, blockIdx.y * per), t_end = min(tiles, t_beg + per);
   const uint32_t r = (uint32_t)(quad * 32) + (uint32_t)(tid & 31);
   uint32_t phase = 0;
   bool ok = true;
   load_tile(bz, a.w3t, HK, c * TN, TN, a.cp, 0, HK);
   load_bias(bias, a.b3, c, a.C);
-  for (uint32_t t = 0; t < tiles; ++t) {
+  for (uint32_t t = t_beg; t < t_end; ++t) {
     const uint32_t row0 = t * TM, row = row0 + r;
     const bool valid_row = row < a.n;
     const uint32_t tgt = valid_row ? a.s[row].target : 0xFFFFFFFFu;
@@ -574,7 +593,7 @@ __global__ void __launch_bounds__(kThreads, 2) out_dw3_kernel(OutArgs a) {
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         // dz^T: element (column cl0 + j, row r)
-        *reinterpret_cast<bf16*>(dzt + koff(cl0 + (uint32_t)j, r, TM)) =
+        *reinterpret_cast<bf16*>(dzt + dzt_off(cl0 + (uint32_t)j, r)) =
             __float2bfloat16_rn(dz_of(v[j], sh, col0 + j, tgt, inv_n));
       }
     }
@@ -585,8 +604,8 @@ __global__ void __launch_bounds__(kThreads, 2) out_dw3_kernel(OutArgs a) {
       tc_after_sync();
 #pragma unroll
       for (int kk = 0; kk < TM / 16; ++kk)
-        mma(d_w, sdesc(su32(dzt) + kk * 256u, TM * 16u), sdesc(su32(bx) + kk * 256u, TM * 16u), idesc(TM, HX),
-            (t > 0 || kk > 0) ? 1u : 0u);
+        mma(d_w, sdesc_lbo(su32(dzt) + kk * 2u * kDztLbo, kDztLbo, kDztSbo), sdesc(su32(bx) + kk * 256u, TM * 16u),
+            idesc(TM, HX), (t > t_beg || kk > 0) ? 1u : 0u);
       commit(&bar);
     }
     if (!bar_wait(&bar, phase)) ok = false;
@@ -598,16 +617,18 @@ __global__ void __launch_bounds__(kThreads, 2) out_dw3_kernel(OutArgs a) {
   // lane r of the accumulator is column c * 128 + r: 64 weight gradients,
   // then the bias gradient; column half 0 takes k 0..31, half 1 k 32..95
   // (the last load reads past the 80 columns, within the allocation)
-  const uint32_t col = c * TN + r;
-  float v[32];
-  for (int q = half; q < (half ? 3 : 1); ++q) {
-    tmem_ld32(d_w + ((uint32_t)(quad * 32) << 16) + (uint32_t)(q * 32), v);
-    if (col < a.C) {
+  if (t_beg < t_end) {
+    const uint32_t col = c * TN + r;
+    float v[32];
+    for (int q = half; q < (half ? 3 : 1); ++q) {
+      tmem_ld32(d_w + ((uint32_t)(quad * 32) << 16) + (uint32_t)(q * 32), v);
+      if (col < a.C) {
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int k = q * 32 + j;
-        if (k < HK) a.dw3[(uint64_t)k * a.C + col] = v[j];
-        else if (k == HK) a.db3[col] = v[j];
+        for (int j = 0; j < 32; ++j) {
+          const int k = q * 32 + j;
+          if (k < HK) atomicAdd(a.dw3 + (uint64_t)k * a.C + col, v[j]);
+          else if (k == HK) atomicAdd(a.db3 + col, v[j]);
+        }
       }
     }
   }
@@ -624,15 +645,25 @@ __global__ void h2x_kernel(const bf16* __restrict__ h2, uint32_t n, uint32_t ldx
   out[i] = __float2bfloat16_rn(v);
 }
 
-// W3 (FP32 master, [64][C]) as the two padded BF16 operands.
-__global__ void w3_operands_kernel(const float* __restrict__ w3, uint32_t C, uint32_t cp, bf16* __restrict__ w3t,
-                                   bf16* __restrict__ w3p) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint64_t)HK * cp) return;
-  const uint32_t k = (uint32_t)(i / cp), c = (uint32_t)(i % cp);
-  const bf16 v = __float2bfloat16_rn(c < C ? w3[(uint64_t)k * C + c] : 0.0f);
-  w3p[i] = v;
-  w3t[(uint64_t)c * HK + k] = v;
+// W3 (FP32 master, [64][C]) as the two padded BF16 operands: W3 itself
+// ([64][cp]) and W3^T ([cp][64]).  One block per 32 columns: W3's rows are
+// read and written along the columns, W3^T's through a shared-memory
+// transpose (one thread per column wrote 2-byte entries 128 bytes apart).
+__global__ void __launch_bounds__(256) w3_operands_kernel(const float* __restrict__ w3, uint32_t C, uint32_t cp,
+                                                          bf16* __restrict__ w3t, bf16* __restrict__ w3p) {
+  __shared__ __align__(4) bf16 t[32][HK + 2];  // [column][k]: rows 132 bytes apart, no bank conflicts
+  const uint32_t c0 = blockIdx.x * 32, tx = threadIdx.x & 31u, ty = threadIdx.x >> 5;
+  const uint32_t c = c0 + tx;
+  for (uint32_t k = ty; k < (uint32_t)HK; k += 8) {
+    const bf16 v = __float2bfloat16_rn(c < C ? w3[(uint64_t)k * C + c] : 0.0f);
+    w3p[(uint64_t)k * cp + c] = v;
+    t[tx][k] = v;
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < 32u * (HK / 2); i += blockDim.x) {
+    const uint32_t cl = i / (HK / 2), kp = i % (HK / 2);
+    reinterpret_cast<uint32_t*>(w3t + (uint64_t)(c0 + cl) * HK)[kp] = *reinterpret_cast<const uint32_t*>(&t[cl][2 * kp]);
+  }
 }
 
 }  // namespace tcm

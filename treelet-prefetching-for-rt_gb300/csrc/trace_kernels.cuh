@@ -76,8 +76,8 @@ struct TraceArgs {
   uint32_t min_votes;          // lanes that must want a treelet before a warp stages it
   const uint32_t* hint;        // staged: predicted next treelet per (treelet, direction octant), or null
   uint32_t wait_tries;         // staged: probes of the wait for the pinned image before staging stops
-  uint32_t tbuf_off;           // byte offset of the trace staging area in dynamic shared memory
-                               // (128-aligned base), kNone: trace entries go straight to the rows
+  uint32_t tbuf_off;           // plain walk: byte offset of the trace staging area in dynamic shared
+                               // memory (128-aligned base), kNone: trace entries go straight to the rows
 };
 
 // Trace staging (the plain walk).  A lane writing its ray's trace rows one
