@@ -281,6 +281,7 @@ def run_reference(args, rank: int, world: int) -> None:
 
 
 TRACE_CAP = 256  # trace entries per ray of the traced timings (visit and treelet-id rows)
+SHORT_STACK = 100  # bench-local mode key: the plain walk with rt_tuning.short_stack = 1
 
 
 def _gpu_words(d_hits, idx) -> np.ndarray:
@@ -348,10 +349,13 @@ def run_gpu(args, rank: int, world: int) -> None:
 
     def launch(mode, rays_d, hits_d, batch, traced):
         apply_tuning(scene, names[mode], batch)
+        scene.set_tuning(short_stack=1 if mode == SHORT_STACK else rt.TUNING_OFF)
+        label = "plain_short_stack" if mode == SHORT_STACK else names[mode]
+        mode = rt.MODE_PLAIN if mode == SHORT_STACK else mode
         # an NVTX range per launch ("staged_bounce", "plain_traced_primary", ...)
         # lets a profiler pick one walk: ncu --nvtx --nvtx-include "<name>/"
         if nvtx:
-            nvtx.range_push(f"{names[mode]}{'_traced' if traced else ''}_{batch}")
+            nvtx.range_push(f"{label}{'_traced' if traced else ''}_{batch}")
         if traced:
             scene.trace(rays_d, hits_d, mode, visits=d_vis, treelets=d_tl, capacity=TRACE_CAP, stream=sp, n=n_prim)
         else:
@@ -431,6 +435,11 @@ def run_gpu(args, rank: int, world: int) -> None:
     # traced timings: every mode writing its visit and treelet-id rows
     for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
         results[name].update(rates(*timed(mode, max(3, args.steps // 4), 1, traced=True), prefix="traced_"))
+    # the plain walk with its warp-synchronous short stack (rt_tuning.short_stack)
+    names[SHORT_STACK] = "plain"
+    results["plain_short_stack"] = rates(*timed(SHORT_STACK, max(3, args.steps // 4), 1))
+    results["plain_short_stack"].update(rates(*timed(SHORT_STACK, max(3, args.steps // 4), 1, traced=True),
+                                              prefix="traced_"))
 
     # roofline of the dominant kernel (the staged walk): algorithmic bytes
     # (the node transactions of its visit traces plus ray and hit) over kernel
@@ -731,6 +740,11 @@ def run_batch(args) -> None:
             from treelet_rt.autotune import autotune_batch
 
             tune = autotune_batch(batch, d_rays, n, mode, reps=2, passes=2, flush=flush)
+            # the per-scene launches it is compared with use the same stack
+            # depth, so that a ray that would overflow a shallower stack does
+            # not make the records differ
+            for s in scenes:
+                s.set_tuning(stack_depth=tune["tuning"]["stack_depth"])
 
         def per_scene():
             for i, s in enumerate(scenes):

@@ -327,6 +327,11 @@ typedef struct rt_tuning {
                                  it; after the last round the rays left finish without queues.  The
                                  scene keeps the queues' device memory (about 64 + 8 * stack_depth + 16
                                  bytes per ray) from the first such launch on. */
+  uint32_t short_stack;       /* RT_MODE_PLAIN over one scene: 1 keeps the bottom 16 entries of each ray's
+                                 stack in shared memory, lane-interleaved per warp (a warp-synchronous
+                                 short stack: entry k of the warp's 32 rays in one row of 32 banks),
+                                 the deeper ones in local memory; RT_TUNING_OFF (the default): the whole
+                                 stack in local memory, about 40% faster on a GB300 */
 } rt_tuning;
 rt_status rt_scene_set_tuning(rt_scene* scene, const rt_tuning* t);
 rt_status rt_scene_get_tuning(const rt_scene* scene, rt_tuning* t);

@@ -38,7 +38,7 @@ def _overflow_expected(peaks: np.ndarray, mode: int, depth: int) -> np.ndarray:
     return (peaks[:, 0] >= depth + 2) | (peaks[:, 1] >= depth + 1)
 
 
-def _check_overflow(ctx, blob, rays, budget, depths):
+def _check_overflow(ctx, blob, rays, budget, depths, tuning=None):
     import treelet_rt as rt
     from oracle import oracle as orc
 
@@ -46,6 +46,8 @@ def _check_overflow(ctx, blob, rays, budget, depths):
     tl = orc.Treelets(bb, budget)
     scene = rt.Scene(ctx, blob)
     scene.form_treelets(budget)
+    if tuning:
+        scene.set_tuning(**tuning)
     flagged_any = 0
     for mode, omode in ((rt.MODE_PLAIN, 0), (rt.MODE_TREELET, 1), (rt.MODE_STAGED, 1)):
         oh, peaks = orc.stack_peaks(bb, rays, omode, tl if omode else None, threads=8)
@@ -64,14 +66,19 @@ def _check_overflow(ctx, blob, rays, budget, depths):
     return flagged_any
 
 
-def test_stack_overflow_deep_chain(ctx):
+@pytest.mark.parametrize("short_stack", [False, True])
+def test_stack_overflow_deep_chain(ctx, short_stack):
     """The plain walk's stack holds 55 leaves at the bottom of an 11-node
-    chain: every ray inside the boxes overflows at depth 48, none at 96."""
+    chain: every ray inside the boxes overflows at depth 48, none at 96.
+    With the warp-synchronous short stack the bottom 16 entries sit in shared
+    memory and the rest in local memory: the same rays overflow, the others
+    equal the oracle."""
     import treelet_rt as rt
 
     blob = rt.Blob.wrap(kat_blob.deep_chain_blob(11))
     rays = kat_blob.grid_rays(16)
-    flagged = _check_overflow(ctx, blob, rays, 8192, (48, 96))
+    flagged = _check_overflow(ctx, blob, rays, 8192, (48, 96),
+                              tuning=dict(short_stack=1) if short_stack else None)
     assert flagged > 0
 
 

@@ -182,6 +182,38 @@ def test_unaligned_trace_rows(ctx):
     scene.close()
 
 
+@pytest.mark.parametrize("cap", [0, 64])
+def test_short_stack_invariance(ctx, cap):
+    """The plain walk's warp-synchronous short stack (the bottom 16 entries of
+    every ray's stack in shared memory, lane-interleaved) changes where stack
+    entries live, never a hit, a visit or a treelet id.  1,500 overlapping
+    triangles push some rays' stacks past 16 entries into the local-memory
+    part."""
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    rng = np.random.default_rng(5)
+    c = rng.uniform(0, 1, (1500, 3)).astype(np.float32)
+    tris = (np.repeat(c, 3, axis=0).reshape(1500, 9) + rng.uniform(-0.25, 0.25, (1500, 9))).astype(np.float32)
+    ident = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [0, 0, 0]], np.float32)
+    blob = rt.Blob.build([tris], [(0, ident, 0)])
+    rays = np.concatenate([rt.camera_rays(rt.default_camera(rt.SCENE_CUBE), 48, 48, 1, 3, 1e-4, 1e30), edge_rays()])
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    scene.set_tuning(short_stack=1, block_threads=128)
+    tl = orc.Treelets(blob.bytes(), 8192)
+    oh, ov, ot = orc.trace(blob.bytes(), rays, 0, tl, capacity=max(cap, 1), want_visits=cap > 0,
+                           want_treelets=cap > 0, threads=8)
+    hits, vis, tids = scene.trace_host(rays, rt.MODE_PLAIN, capacity=cap, want_visits=cap > 0, want_treelets=cap > 0)
+    assert_hits_equal(hits, oh, "plain walk with the short stack")
+    if cap:
+        assert_traces_equal(vis, ov, oh["n_visits"], "visits, short stack")
+        assert_traces_equal(tids, ot, oh["n_visits"], "treelet ids, short stack")
+    _, peaks = orc.stack_peaks(blob.bytes(), rays, 0, None, threads=8)
+    assert (peaks[:, 0] > 16).any(), "no ray reached the local-memory part of the stack"
+    scene.close()
+
+
 @pytest.mark.parametrize("tuning", [dict(staged_slots=1, staged_epoch=1, staged_min_votes=1),
                                     dict(staged_slots=8, staged_epoch=4, staged_slot_bytes=1024),
                                     dict(staged_slots=2, staged_epoch=64, staged_threads=256, staged_min_votes=8),

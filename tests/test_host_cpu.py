@@ -188,3 +188,15 @@ def test_prefetch_queue_limit_and_second_prefetch():
 def test_prefetch_empty_lanes():
     d, st = _decide(next_unit=np.full(5, NONE, np.uint32), heuristic=1)
     assert d["treelet"] == NONE and d["submitted"] == 0 and st["last_rejected"] == NONE
+
+
+def test_set_tuning_takes_every_tuning_field():
+    """Scene.set_tuning names every field of the C struct rt_tuning (the
+    autotuner passes whole configurations as keywords)."""
+    import inspect
+
+    import treelet_rt as rt
+    from treelet_rt._ffi import Tuning
+
+    params = set(inspect.signature(rt.Scene.set_tuning).parameters) - {"self"}
+    assert params == {name for name, _ in Tuning._fields_}

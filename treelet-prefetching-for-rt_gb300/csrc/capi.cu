@@ -136,7 +136,7 @@ struct rt_scene {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;  // ray hand-out counter of the persistent kernels
-  rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096, rtk::kWaitTries, RT_TUNING_OFF};
+  rt_tuning tuning{128, 256, 16, RT_TUNING_OFF, 8, 2048, 8, 96, 4096, rtk::kWaitTries, RT_TUNING_OFF, RT_TUNING_OFF};
   // host-buffer path: a copy-in stream, two trace streams (chunk c on
   // stream / stream2 by parity, so one chunk's launch fills the SMs that the
   // previous chunk's last rays leave idle), a copy-out stream, and events
@@ -345,6 +345,11 @@ rt_status merge_tuning(const rt_tuning& cur, const rt_tuning* t, rt_tuning& n) {
       return rti::fail(RT_ERR_INVALID, "queue_rounds must be 1..64 or RT_TUNING_OFF");
     n.queue_rounds = t->queue_rounds;
   }
+  if (t->short_stack) {
+    if (t->short_stack != 1 && t->short_stack != RT_TUNING_OFF)
+      return rti::fail(RT_ERR_INVALID, "short_stack must be 1 or RT_TUNING_OFF");
+    n.short_stack = t->short_stack;
+  }
   return RT_OK;
 }
 
@@ -430,17 +435,29 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
   // (TRACED).  The plain walk writes its rows a whole 32-byte sector at a
   // time through shared memory (rtk::trace_put) when every row starts on a
   // 32-byte boundary, else entry by entry; the treelet walks write entry by
-  // entry.
+  // entry (staging their rows through shared memory, inline at each
+  // recording site or through a per-lane ring written once per node visit,
+  // measured 5-31% slower on their traced launches).
   const bool traced = a.cap != 0;
   const bool stage_rows = traced && mode == RT_MODE_PLAIN && (a.cap % 8u) == 0 &&
                           ((uintptr_t)a.visits & 31u) == 0 && ((uintptr_t)a.tl_trace & 31u) == 0;
+  const uint32_t stage_warp_bytes = rtk::kTraceBufWarpBytes;
   a.tbuf_off = rtk::kNone;
+  a.ss_off = rtk::kNone;
   if (mode == RT_MODE_PLAIN || mode == RT_MODE_TREELET) {
     const uint32_t bt = t.block_threads;
-    const size_t dyn = stage_rows ? (size_t)(bt / 32) * rtk::kTraceBufWarpBytes + 128 : 0;
+    size_t dyn = stage_rows ? (size_t)(bt / 32) * stage_warp_bytes + 128 : 0;
     if (stage_rows) a.tbuf_off = 0;
+    // the warp-synchronous short stack, after the trace staging area
+    const bool short_stack = mode == RT_MODE_PLAIN && !a.n_items && t.short_stack == 1;
+    if (short_stack) {
+      a.ss_off = stage_rows ? (uint32_t)(bt / 32) * stage_warp_bytes : 0u;
+      dyn = a.ss_off + (size_t)(bt / 32) * rtk::kShortStackWarpBytes + 128;
+    }
     void (*kern)(rtk::TraceArgs);
-    if (mode == RT_MODE_PLAIN)
+    if (short_stack)
+      kern = traced ? rtk::trace_plain_kernel<CAP, false, true, true> : rtk::trace_plain_kernel<CAP, false, false, true>;
+    else if (mode == RT_MODE_PLAIN)
       kern = a.n_items ? (traced ? rtk::trace_plain_kernel<CAP, true, true> : rtk::trace_plain_kernel<CAP, true, false>)
                        : (traced ? rtk::trace_plain_kernel<CAP, false, true> : rtk::trace_plain_kernel<CAP, false, false>);
     else
@@ -1203,7 +1220,8 @@ struct rt_batch {
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
   uint32_t* d_queue = nullptr;
-  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, RT_TUNING_OFF, rtk::kWaitTries, RT_TUNING_OFF};  // batches pin nothing
+  rt_tuning tuning{128, 128, 16, 1, 8, 2048, 2, 96, RT_TUNING_OFF, rtk::kWaitTries, RT_TUNING_OFF,
+                   RT_TUNING_OFF};  // batches pin nothing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };

@@ -76,8 +76,9 @@ struct TraceArgs {
   uint32_t min_votes;          // lanes that must want a treelet before a warp stages it
   const uint32_t* hint;        // staged: predicted next treelet per (treelet, direction octant), or null
   uint32_t wait_tries;         // staged: probes of the wait for the pinned image before staging stops
-  uint32_t tbuf_off;           // plain walk: byte offset of the trace staging area in dynamic shared
-                               // memory (128-aligned base), kNone: trace entries go straight to the rows
+  uint32_t tbuf_off;           // byte offset of the trace staging area in dynamic shared memory
+                               // (128-aligned base), kNone: trace entries go straight to the rows
+  uint32_t ss_off;             // plain walk with SHORT: byte offset of the short stacks, likewise
 };
 
 // Trace staging (the plain walk).  A lane writing its ray's trace rows one
@@ -319,9 +320,17 @@ __device__ __forceinline__ void run_persistent(const TraceArgs& a, W& w, unsigne
 // the internal node descended next (the first hit internal child, :2570-2578);
 // leaves and further children are pushed.  A top-level instance leaf is
 // followed by its whole BLAS before the next top-level entry (:2602-2679).
+// The warp-synchronous short stack (SHORT): entries 0..kShortStack-1 of each
+// ray's stack in its warp's shared memory, entry k of the warp's 32 rays in
+// one 128-byte row (lane l in bank l, so a warp's pushes and pops at any mix
+// of depths never conflict), the deeper entries in the local-memory stack.
+constexpr int kShortStack = 16;
+constexpr uint32_t kShortStackWarpBytes = kShortStack * 32 * 4;
+
 // TRACED = false compiles the walk of a launch without traces (no trace
-// code at all); TRACED = true writes the rows.
-template <int CAP, bool MULTI, bool TRACED>
+// code at all); TRACED = true writes the rows.  SHORT keeps the bottom of the
+// stack in shared memory (rt_tuning.short_stack).
+template <int CAP, bool MULTI, bool TRACED, bool SHORT = false>
 struct PlainWalker {
   rtm::V3 O, D, idir;
   float tmin, tmax, min_thit, c_tobj;
@@ -336,12 +345,21 @@ struct PlainWalker {
 
   __device__ __forceinline__ bool active() const { return next != kNone || sp > 0; }
 
-  __device__ __forceinline__ void push(uint32_t e) {
-    if (sp < CAP) stk[sp++] = e;
+
+  // entry i of the stack (the short stack's rows for i < kShortStack)
+  __device__ __forceinline__ uint32_t* slot(const TraceArgs& a, int i) {
+    if (SHORT && i < kShortStack) {
+      uint8_t* base = rt_dyn_smem + ((128u - ((uint32_t)__cvta_generic_to_shared(rt_dyn_smem) & 127u)) & 127u);
+      return reinterpret_cast<uint32_t*>(base + a.ss_off + (threadIdx.x >> 5) * kShortStackWarpBytes) +
+             i * 32 + (threadIdx.x & 31u);
+    }
+    return stk + i;
+  }
+  __device__ __forceinline__ void push(const TraceArgs& a, uint32_t e) {
+    if (sp < CAP) *slot(a, sp++) = e;
     else status |= RT_RAY_STACK_OVERFLOW;
   }
-
-  __device__ __forceinline__ uint32_t pop() { return stk[--sp]; }
+  __device__ __forceinline__ uint32_t pop(const TraceArgs& a) { return *slot(a, --sp); }
 
   __device__ __forceinline__ void init(const TraceArgs& a, uint32_t r) {
     v = scene_of<MULTI>(a, r);
@@ -368,7 +386,7 @@ struct PlainWalker {
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
     const rtm::V3 bmax = rtm::v3(__uint_as_float(h1.y), __uint_as_float(h1.z), __uint_as_float(h1.w));
     float th;
-    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) push(((uint32_t)(root_off >> 6) << 2) | kTop);
+    if (rtm::ray_box_test(bmin, bmax, idir, O, tmin, tmax, th)) push(a, ((uint32_t)(root_off >> 6) << 2) | kTop);
   }
 
   __device__ __forceinline__ void stop(uint32_t bits) {
@@ -396,7 +414,7 @@ struct PlainWalker {
       const uint32_t info = ch.info_of(i);
       const bool h = (ch.hit_mask >> i) & 1u, internal = (info >> 2) == rtf::CT_INTERNAL;
       const bool take = h && internal && nn == kNone, store = h && !take, ok = sp < CAP;
-      if (store && ok) stk[sp] = (c << 2) | level | (internal ? 0u : kLeaf);
+      if (store && ok) *slot(a, sp) = (c << 2) | level | (internal ? 0u : kLeaf);
       if (store && !ok) status |= RT_RAY_STACK_OVERFLOW;
       sp += (store && ok) ? 1 : 0;
       nn = take ? c : nn;
@@ -443,7 +461,7 @@ struct PlainWalker {
     const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
     enter_instance(in, unit, O, D, tmin, tmax, ic);
     ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
-    push((uint32_t)(broot >> 6) << 2);
+    push(a, (uint32_t)(broot >> 6) << 2);
     inblas = true;
     if (status & RT_RAY_STACK_OVERFLOW) stop(0);
     return (uint32_t)(hdr >> 6);
@@ -461,8 +479,8 @@ struct PlainWalker {
         break;
       }
       if (inblas) {
-        if (sp > 0 && !(stk[sp - 1] & kTop)) {
-          const uint32_t e = pop();
+        if (sp > 0 && !(*slot(a, sp - 1) & kTop)) {
+          const uint32_t e = pop(a);
           if (e & kLeaf) {
             unit = e >> 2;
             kind = 1;
@@ -475,7 +493,7 @@ struct PlainWalker {
         continue;
       }
       if (sp == 0) return;
-      const uint32_t e = pop();
+      const uint32_t e = pop(a);
       if (!(e & kLeaf)) {
         next = e >> 2;
         continue;
@@ -517,9 +535,9 @@ struct PlainWalker {
 // slower traced on bounce rays).
 // Its fields in registers (90, or capped at 51-85 with spills) measured
 // 40-45% slower, while the treelet walks gained from them (below).
-template <int CAP, bool MULTI, bool TRACED>
+template <int CAP, bool MULTI, bool TRACED, bool SHORT = false>
 __global__ void __launch_bounds__(256, 5) trace_plain_kernel(TraceArgs a) {
-  PlainWalker<CAP, MULTI, TRACED> w;
+  PlainWalker<CAP, MULTI, TRACED, SHORT> w;
   unsigned long long bytes = 0;
   run_persistent(a, w, bytes);
   if (a.stats) add_warp_total64(a.stats + ST_NODE_BYTES, bytes);

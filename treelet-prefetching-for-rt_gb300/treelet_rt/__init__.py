@@ -263,10 +263,10 @@ class Scene:
 
     def set_tuning(self, block_threads=0, staged_threads=0, staged_epoch=0, staged_slots=0, refill_lanes=0,
                    staged_slot_bytes=0, staged_min_votes=0, stack_depth=0, pinned_bytes=0, wait_tries=0,
-                   queue_rounds=0) -> None:
-        """0 keeps a value; TUNING_OFF switches staged_slots / pinned_bytes / queue_rounds off."""
+                   queue_rounds=0, short_stack=0) -> None:
+        """0 keeps a value; TUNING_OFF switches staged_slots / pinned_bytes / queue_rounds / short_stack off."""
         t = Tuning(block_threads, staged_threads, staged_epoch, staged_slots, refill_lanes, staged_slot_bytes,
-                   staged_min_votes, stack_depth, pinned_bytes, wait_tries, queue_rounds)
+                   staged_min_votes, stack_depth, pinned_bytes, wait_tries, queue_rounds, short_stack)
         check(lib().rt_scene_set_tuning(self._h, C.byref(t)))
 
     def set_pin_order(self, order=None) -> None:

@@ -54,7 +54,7 @@ class Tuning(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("staged_threads", C.c_uint32), ("staged_epoch", C.c_uint32),
                 ("staged_slots", C.c_uint32), ("refill_lanes", C.c_uint32), ("staged_slot_bytes", C.c_uint32),
                 ("staged_min_votes", C.c_uint32), ("stack_depth", C.c_uint32), ("pinned_bytes", C.c_uint32),
-                ("wait_tries", C.c_uint32), ("queue_rounds", C.c_uint32)]
+                ("wait_tries", C.c_uint32), ("queue_rounds", C.c_uint32), ("short_stack", C.c_uint32)]
 
 
 TUNING_OFF = 0xFFFFFFFF

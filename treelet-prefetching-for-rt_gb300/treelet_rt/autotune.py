@@ -35,9 +35,11 @@ GRID_STAGED = {
     "stack_depth": [48, 96, 160],
     "queue_rounds": [OFF, 1, 2, 4],
 }
+# the plain walk also tries its warp-synchronous short stack
+GRID_PLAIN = {**GRID_COMMON, "short_stack": [OFF, 1]}
 DEFAULTS = {"block_threads": 128, "staged_threads": 256, "staged_epoch": 16, "staged_slots": OFF, "refill_lanes": 8,
             "staged_slot_bytes": 2048, "staged_min_votes": 8, "stack_depth": 96, "pinned_bytes": 4096,
-            "queue_rounds": OFF}
+            "queue_rounds": OFF, "short_stack": OFF}
 
 
 def stages(cfg: dict) -> bool:
@@ -83,7 +85,7 @@ def autotune(scene, d_rays, n: int, mode: int, budgets=None, reps: int = 2, pass
     import treelet_rt as rt
 
     d_hits = torch.empty(n * 64, dtype=torch.uint8, device=d_rays.device)
-    grid = GRID_STAGED if mode == rt.MODE_STAGED else GRID_COMMON
+    grid = GRID_STAGED if mode == rt.MODE_STAGED else (GRID_PLAIN if mode == rt.MODE_PLAIN else GRID_COMMON)
     best = dict(DEFAULTS)
     table = []
     budget = None
