@@ -1224,6 +1224,11 @@ struct rt_batch {
                    RT_TUNING_OFF};  // batches pin nothing
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // staged batches: item launches spread over side streams (one per scene
+  // index modulo kBatchLanes), forked from and joined to the caller's stream
+  static constexpr uint32_t kBatchLanes = 8;
+  cudaStream_t lane[kBatchLanes] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kBatchLanes] = {};
 };
 
 namespace {
@@ -1279,19 +1284,40 @@ rt_status batch_args(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uin
 // queues, whose memory a scene grows on demand), one launch per item in
 // order on `st`.  A CTA's shared memory holds one scene's treelets, so the
 // items are not merged into one persistent launch as the other modes are.
+// A staged batch runs each item as its scene's own staged launch (a CTA's
+// shared memory holds one scene's pinned treelets).  The launches go to
+// kBatchLanes side streams forked from `st` (and joined back), so that the
+// launches of small items, whose persistent grids leave SMs free, run side by
+// side: a scene's items all go to one lane, in item order, since they share
+// the scene's ray counter and statistics.  The fork and join are recorded
+// into a graph when `st` is being captured.
 rt_status batch_staged(rt_batch* b, const rt_ray* rays, const uint32_t* flags, uint32_t default_flags, rt_hit* hits,
                        cudaStream_t st) {
-  for (uint32_t k = 0; k < b->n_items; ++k) {
+  if (!b->ev_fork) {
+    for (uint32_t j = 0; j < rt_batch::kBatchLanes; ++j) {
+      RT_CUDA(cudaStreamCreateWithFlags(&b->lane[j], cudaStreamNonBlocking));
+      RT_CUDA(cudaEventCreateWithFlags(&b->ev_join[j], cudaEventDisableTiming));
+    }
+    RT_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  }
+  RT_CUDA(cudaEventRecord(b->ev_fork, st));
+  for (uint32_t j = 0; j < rt_batch::kBatchLanes; ++j) RT_CUDA(cudaStreamWaitEvent(b->lane[j], b->ev_fork, 0));
+  rt_status r = RT_OK;
+  for (uint32_t k = 0; k < b->n_items && r == RT_OK; ++k) {
     const uint32_t lo = b->item_begin[k], m = b->item_begin[k + 1] - lo;
     if (m == 0) continue;
     rt_scene* s = b->scenes[b->item_scene[k]];
-    rt_status r = check_trace(s, RT_MODE_STAGED, nullptr, "rt_trace_batch");
-    if (r != RT_OK) return r;
-    r = trace_launch(s, rays + lo, flags ? flags + lo : nullptr, default_flags, m, RT_MODE_STAGED, hits + lo, nullptr,
-                     st, s->d_queue, false, false);
-    if (r != RT_OK) return r;
+    r = check_trace(s, RT_MODE_STAGED, nullptr, "rt_trace_batch");
+    if (r == RT_OK)
+      r = trace_launch(s, rays + lo, flags ? flags + lo : nullptr, default_flags, m, RT_MODE_STAGED, hits + lo,
+                       nullptr, b->lane[b->item_scene[k] % rt_batch::kBatchLanes], s->d_queue, false, false);
   }
-  return RT_OK;
+  // join every lane back, also after a failure (a capture must end joined)
+  for (uint32_t j = 0; j < rt_batch::kBatchLanes; ++j) {
+    RT_CUDA(cudaEventRecord(b->ev_join[j], b->lane[j]));
+    RT_CUDA(cudaStreamWaitEvent(st, b->ev_join[j], 0));
+  }
+  return r;
 }
 
 }  // namespace
@@ -1335,6 +1361,11 @@ rt_status rt_batch_create(rt_ctx* ctx, rt_scene* const* scenes, uint32_t n_scene
 rt_status rt_batch_destroy(rt_batch* b) {
   if (!b) return RT_OK;
   free_graph(b);
+  for (uint32_t j = 0; j < rt_batch::kBatchLanes; ++j) {
+    if (b->lane[j]) cudaStreamDestroy(b->lane[j]);
+    if (b->ev_join[j]) cudaEventDestroy(b->ev_join[j]);
+  }
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   cudaFree(b->d_views);
   cudaFree(b->d_item_begin);
   cudaFree(b->d_item_scene);
