@@ -1538,11 +1538,16 @@ extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const
   RT_CUDA(cudaSetDevice(s->ctx->device));
   const uint32_t cap = row_capacity;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  // four equal chunks from 2^19 rays on (a queued staged launch runs whole:
+  // its queues are the scene's, one set)
   uint64_t bound[rti::kHostChunks + 1];
   uint32_t chunks = 1;
   bound[0] = 0;
   bound[1] = n;
-  if (!queued(s, mode)) chunks = rti::host_chunk_bounds(n, bound);
+  if (!queued(s, mode) && n >= (1u << 19)) {
+    chunks = rti::kHostChunks;
+    for (uint32_t c = 0; c <= chunks; ++c) bound[c] = (uint64_t)n * c / chunks;
+  }
   const size_t b_rays = al(sizeof(rt_ray) * (size_t)n), b_flags = flags ? al(sizeof(uint32_t) * (size_t)n) : 0;
   const size_t b_hits = al(sizeof(rt_hit) * (size_t)n), b_row = al(sizeof(uint32_t) * (size_t)n * cap);
   const size_t b_cnt = al(sizeof(uint32_t) * (size_t)n);
@@ -1587,21 +1592,27 @@ extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const
   RT_CUDA(cudaMemsetAsync(s->d_stats, 0, sizeof(unsigned long long) * rtk::ST_COUNT, s->xin));
   RT_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(uint32_t), s->xin));
   cudaError_t e = cudaSuccess;
-  // every chunk's rays in, trace, counts, offsets and total
-  for (uint32_t c = 0; c < chunks && e == cudaSuccess && st == RT_OK; ++c) {
+  // every chunk's rays in
+  for (uint32_t c = 0; c < chunks && e == cudaSuccess; ++c) {
     const size_t lo = bound[c];
     const uint32_t m = (uint32_t)(bound[c + 1] - bound[c]);
     e = cudaMemcpyAsync(d_rays + lo, rays + lo, sizeof(rt_ray) * m, cudaMemcpyHostToDevice, s->xin);
     if (e == cudaSuccess && flags)
       e = cudaMemcpyAsync(d_flags + lo, flags + lo, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, s->xin);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev_in[c], s->xin);
+  }
+  // chunk c's trace, counts, offsets and total (copied to the page-locked
+  // h_tot[c]), ending in ev_done[c]
+  auto trace_chunk = [&](uint32_t c) -> bool {
+    const size_t lo = bound[c];
+    const uint32_t m = (uint32_t)(bound[c + 1] - bound[c]);
     cudaStream_t cs = (c & 1) ? s->stream2 : s->stream;
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, s->ev_in[c], 0);
-    if (e != cudaSuccess) break;
+    e = cudaStreamWaitEvent(cs, s->ev_in[c], 0);
+    if (e != cudaSuccess) return false;
     rt_trace_buf rows{d_vis ? d_vis + lo * cap : nullptr, d_tl ? d_tl + lo * cap : nullptr, cap};
     st = trace_launch(s, d_rays + lo, d_flags ? d_flags + lo : nullptr, default_flags, m, mode, d_hits + lo, &rows, cs,
                       s->d_queue + c, true);
-    if (st != RT_OK) break;
+    if (st != RT_OK) return false;
     const uint32_t nb = (m + rtk::kBinScanItems - 1) / rtk::kBinScanItems;
     uint32_t* blk = d_blk + c * blk_stride;
     trace_counts_kernel<<<(m + 255) / 256, 256, 0, cs>>>(d_hits + lo, m, cap, d_cnt + lo);
@@ -1612,10 +1623,15 @@ extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->h_tot + c, d_tot + c, sizeof(unsigned long long), cudaMemcpyDeviceToHost, cs);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev_done[c], cs);
-  }
-  // in chunk order: the chunk's total, then its packing and copies
+    return e == cudaSuccess;
+  };
+  // In chunk order: wait for chunk c's total, queue its packing and copies,
+  // then queue chunk c + 1's trace, so that the GPU runs the short pack
+  // kernel before the next persistent trace fills the SMs and the copies
+  // overlap that trace.
   unsigned long long base = 0;
   bool fits = true;
+  if (e == cudaSuccess) trace_chunk(0);
   for (uint32_t c = 0; c < chunks && e == cudaSuccess && st == RT_OK; ++c) {
     const size_t lo = bound[c];
     const uint32_t m = (uint32_t)(bound[c + 1] - bound[c]);
@@ -1645,12 +1661,11 @@ extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const
     e = cudaStreamWaitEvent(s->xout, s->ev_done[c], 0);
     if (e != cudaSuccess) break;
     unsigned long long* goff = d_goff + lo;
-    // 128-thread blocks, few registers: they fit beside the persistent trace
-    // of the next chunk on an SM instead of waiting for it to end
     trace_pack_kernel<<<std::min<uint32_t>((m + 3) / 4, 152 * 8), 128, 0, s->xout>>>(
         d_vis ? d_vis + lo * cap : nullptr, d_tl ? d_tl + lo * cap : nullptr, d_off + lo, m, cap, (uint32_t)tot_c, base,
         goff, dst_vis, dst_tl);
     e = cudaGetLastError();
+    if (e == cudaSuccess && c + 1 < chunks && !trace_chunk(c + 1)) break;
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(hits + lo, d_hits + lo, sizeof(rt_hit) * m, cudaMemcpyDeviceToHost, s->xout);
     if (e == cudaSuccess)
