@@ -302,7 +302,7 @@ __device__ __forceinline__ void run_persistent(const TraceArgs& a, W& w, unsigne
       continue;
     }
     if (have) {
-      w.step(a);
+      w.step(a, r);
       if (!w.active()) {
         w.finish(a, r);
         bytes += w.rec.bytes;
@@ -520,6 +520,9 @@ struct PlainWalker {
     }
     if (unit2 != kNone) rec.rec<TRACED>(a, unit2, type2);
   }
+
+  // (the walk keeps its own rows in the recorder; the ray index is not needed)
+  __device__ __forceinline__ void step(const TraceArgs& a, uint32_t) { step(a); }
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
     const bool bad = status & (RT_RAY_STACK_OVERFLOW | RT_RAY_BAD_NODE);

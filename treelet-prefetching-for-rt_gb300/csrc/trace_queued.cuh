@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_que
         continue;
       }
       if (have) {
-        w.step(a, lookup);
+        w.step(a, r, lookup);
         if (!w.active()) {
           w.finish(a, r);
           bytes += w.rec.bytes;
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_que
       bool go = live;
       while (__any_sync(0xffffffffu, go)) {
         if (go) {
-          w.step(a, lookup);
+          w.step(a, r, lookup);
           go = w.in_treelet();
         }
       }

@@ -28,13 +28,15 @@ constexpr uint32_t kRouteOther = 6, kRouteInst = 12;  // route bits (treelets.h)
 //
 // Fields a step rarely needs live in the tail of the stack array, in local
 // memory, instead of registers (kColdWords 64-bit words after the 2 CAP stack
-// entries): the world direction, the closest hit, the trace rows and, in the
-// unstaged walk, the world origin and inverse direction, which only TLAS
-// nodes and instance entries read.  Fewer live registers let the treelet
+// entries): the world direction, the closest hit and, in the unstaged walk,
+// the world origin and inverse direction, which only TLAS nodes and instance
+// entries read.  The trace rows are found from the ray index, which the
+// kernel's loop holds anyway, instead of from the tail (two local loads per
+// recorded transaction before).  Fewer live registers let the treelet
 // walk run four CTAs per SM at 64 registers: +5% on bounce rays, +2% on
 // primary rays; the staged walk, with its pinned-record state, measured best
 // with the world ray in registers at three CTAs per SM.
-constexpr int kColdWords = 9;
+constexpr int kColdWords = 7;
 
 // SLAB = true keeps the other-treelet stack in a per-ray slab of global
 // memory (`ot`, CAP entries) instead of the local array, so that a ray can
@@ -98,9 +100,9 @@ struct Walker {
   }
   __device__ __forceinline__ void set_world(rtm::V3 o, rtm::V3 id) {
     if (kColdWorld) {
-      cold(6) = pack(o.x, o.y);
-      cold(7) = pack(o.z, id.x);
-      cold(8) = pack(id.y, id.z);
+      cold(4) = pack(o.x, o.y);
+      cold(5) = pack(o.z, id.x);
+      cold(6) = pack(id.y, id.z);
     } else {
       O = o;
       idir = id;
@@ -108,24 +110,23 @@ struct Walker {
   }
   __device__ __forceinline__ rtm::V3 world_o() const {
     if (!kColdWorld) return O;
-    const unsigned long long a = cold(6), b = cold(7);
+    const unsigned long long a = cold(4), b = cold(5);
     return rtm::v3(lo(a), hi(a), lo(b));
   }
   __device__ __forceinline__ rtm::V3 world_idir() const {
     if (!kColdWorld) return idir;
-    const unsigned long long b = cold(7), c = cold(8);
+    const unsigned long long b = cold(5), c = cold(6);
     return rtm::v3(hi(b), lo(c), hi(c));
   }
   // one visit of the trace (the reference's MemoryTransactionRecord)
   // The rows are written entry by entry: staging them through shared memory
   // as the plain walk does measured 15-30% slower here (eight inlined
   // copies of the staging code in the traced walk).
-  __device__ __forceinline__ void record(const TraceArgs& a, uint32_t unit, uint32_t type) {
+  __device__ __forceinline__ void record(const TraceArgs& a, uint32_t r, uint32_t unit, uint32_t type) {
     if (TRACED && rec.n < rec.cap) {
-      uint32_t* vrow = reinterpret_cast<uint32_t*>(cold(4));
-      uint32_t* trow = reinterpret_cast<uint32_t*>(cold(5));
-      if (vrow) vrow[rec.n] = rtf::pack_visit(unit, type);
-      if (trow) trow[rec.n] = v.meta[unit].x;
+      const uint64_t at = (uint64_t)r * a.cap + rec.n;
+      if (a.visits) a.visits[at] = rtf::pack_visit(unit, type);
+      if (a.tl_trace) a.tl_trace[at] = v.meta[unit].x;
     }
     rec.n++;
     rec.bytes += rtf::tx_bytes(type);
@@ -173,8 +174,6 @@ struct Walker {
     load_ray(a.rays, r, o, tmin, D, tmax);
     const uint32_t flags = a.flags ? a.flags[r] : a.default_flags;
     terminate = flags & rtf::RAY_FLAG_TERMINATE_ON_FIRST_HIT;
-    cold(4) = reinterpret_cast<unsigned long long>(a.visits ? a.visits + (uint64_t)r * a.cap : nullptr);
-    cold(5) = reinterpret_cast<unsigned long long>(a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr);
     rec = Counts{a.cap, 0u, 0u};
     status = 0;
     clear();
@@ -187,7 +186,7 @@ struct Walker {
     set_world(o, id);
     fast = rtd::finite_ray(o, D, tmin, tmax);
     ic_fast = false;
-    record(a, 0, rtf::TX_STRUCTURE);
+    record(a, r, 0, rtf::TX_STRUCTURE);
     const uint4 h0 = __ldg(v.blob), h1 = __ldg(v.blob + 1);
     const uint64_t root_off = (uint64_t)h0.x | ((uint64_t)h0.y << 32);
     const rtm::V3 bmin = rtm::v3(__uint_as_float(h0.z), __uint_as_float(h0.w), __uint_as_float(h1.x));
@@ -234,8 +233,6 @@ struct Walker {
     rec = Counts{a.cap, q2.z, q2.w};
     cold(2) = (unsigned long long)q3.x | ((unsigned long long)q3.y << 32);
     cold(3) = (unsigned long long)q3.z;
-    cold(4) = reinterpret_cast<unsigned long long>(a.visits ? a.visits + (uint64_t)r * a.cap : nullptr);
-    cold(5) = reinterpret_cast<unsigned long long>(a.tl_trace ? a.tl_trace + (uint64_t)r * a.cap : nullptr);
     nxt = 0;
     ncu = 0;
     not_ = (int)q3.w;
@@ -254,7 +251,7 @@ struct Walker {
   // Visits one node; `lookup(unit, meta)` returns the shared-memory address
   // of a node staged in a warp slot, else 0.
   template <class Lookup>
-  __device__ __forceinline__ void step(const TraceArgs& a, Lookup&& lookup) {
+  __device__ __forceinline__ void step(const TraceArgs& a, uint32_t r, Lookup&& lookup) {
     const bool from_cu = nxt != 0 || ncu > 0;  // :1748-1754
     unsigned long long e = nxt;
     if (!nxt) {
@@ -323,7 +320,7 @@ struct Walker {
       ic_fast = rtd::finite_ray(ic.o, ic.d, ic.tmin, ic.tmax);
     }
     if (!leaf) {  // internal node, top (:1758-1869) or bottom (:1954-2070)
-      record(a, unit, rtf::TX_INTERNAL);
+      record(a, r, unit, rtf::TX_INTERNAL);
       uint32_t soff01 = 0, soff23 = 0, soff45 = 0;
       if (pinned) {  // route bits in bytes 16..17, child records in the tail
         const uint4 t = rtd::ld_shared_v4(saddr + rtp::IN_UNIT);
@@ -359,7 +356,7 @@ struct Walker {
         c += ci & 3u;
       }
     } else if (top) {  // instance leaf (:1870-1953)
-      record(a, unit, rtf::TX_INSTANCE_LEAF);
+      record(a, r, unit, rtf::TX_INSTANCE_LEAF);
       uint32_t hdr_unit, broot_unit, broot_soff = 0;
       if (pinned) {  // the 64-byte record: units, route bits, BLAS root record, rows
         hdr_unit = nd.w[rtp::IL_HDR_UNIT / 4];
@@ -375,11 +372,11 @@ struct Walker {
         const uint64_t broot = hdr + ((uint64_t)h0.x | ((uint64_t)h0.y << 32));
         broot_unit = (uint32_t)(broot >> 6);
       }
-      record(a, hdr_unit, rtf::TX_STRUCTURE);
+      record(a, r, hdr_unit, rtf::TX_STRUCTURE);
       const uint32_t cc = broot_soff ? ((broot_soff << kEShift) | kEPin) : (broot_unit << kEShift);
       push((rbits >> (kRouteInst + rsh)) & 1u, cc, unit);
     } else {  // primitive leaf (:2071-2196)
-      record(a, unit, rtf::TX_LEAF_DESC);
+      record(a, r, unit, rtf::TX_LEAF_DESC);
       const rtd::Node64& q = nd;
       if (rtf::leaf_type_of(q.w[1]) == 0) {
         const rtm::V3 v0 = rtm::v3(__uint_as_float(q.w[4]), __uint_as_float(q.w[5]), __uint_as_float(q.w[6]));
@@ -391,21 +388,21 @@ struct Walker {
         if (hit && tmin <= wt && wt <= tmax && wt < min_thit) {  // :2127-2141
           min_thit = t / ic.mult;
           set_hit(unit, inst, t);
-          record(a, unit, rtf::TX_QUAD_LEAF_HIT);
+          record(a, r, unit, rtf::TX_QUAD_LEAF_HIT);
           if (terminate) clear();
         } else {
-          record(a, unit, rtf::TX_QUAD_LEAF);
+          record(a, r, unit, rtf::TX_QUAD_LEAF);
         }
       } else {
         status |= RT_RAY_HIT_PROCEDURAL;
-        record(a, unit, rtf::TX_PROCEDURAL_LEAF);
+        record(a, r, unit, rtf::TX_PROCEDURAL_LEAF);
       }
     }
     if (status & RT_RAY_STACK_OVERFLOW) clear();
   }
 
-  __device__ __forceinline__ void step(const TraceArgs& a) {
-    step(a, [](uint32_t, const uint2*) -> uint32_t { return 0u; });
+  __device__ __forceinline__ void step(const TraceArgs& a, uint32_t r) {
+    step(a, r, [](uint32_t, const uint2*) -> uint32_t { return 0u; });
   }
 
   __device__ __forceinline__ void finish(const TraceArgs& a, uint32_t r) {
@@ -663,8 +660,8 @@ __global__ void __launch_bounds__(kStagedMaxThreads, kStagedMinBlocks) trace_sta
     }
     // --- one node visit per lane
     if (have) {
-      if (SLOTS) w.step(a, lookup);
-      else w.step(a);
+      if (SLOTS) w.step(a, r, lookup);
+      else w.step(a, r);
       if (!w.active()) {
         w.finish(a, r);
         bytes += w.rec.bytes;
