@@ -134,9 +134,10 @@ def test_hand_derived_edge_cases(ctx):
 
 @pytest.mark.parametrize("cap", [6, 8, 16])
 def test_trace_overflow_truncates(ctx, cap):
-    """Rows shorter than the traces: capacities that are not a multiple of 8
-    are written entry by entry, multiples of 8 a 32-byte sector at a time
-    through shared memory; both keep each ray's first `cap` entries."""
+    """Rows shorter than the traces: the plain walk writes capacities that
+    are not a multiple of 8 entry by entry and multiples of 8 a 32-byte
+    sector at a time through shared memory (the treelet walks entry by entry
+    always); every walk keeps each ray's first `cap` entries."""
     import treelet_rt as rt
 
     blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 4096, 9)
@@ -147,8 +148,9 @@ def test_trace_overflow_truncates(ctx, cap):
 
 def test_unaligned_trace_rows(ctx):
     """Device rows that do not start on a 32-byte boundary (an offset of one
-    entry into the caller's buffer) take the entry-by-entry stores; rows that
-    do take the staged sector writes: both equal the oracle."""
+    entry into the caller's buffer) take the entry-by-entry stores; in the
+    plain walk rows that do take the sector writes staged through shared
+    memory: every walk equals the oracle either way."""
     import torch
 
     import treelet_rt as rt
