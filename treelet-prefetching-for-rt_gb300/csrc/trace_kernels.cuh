@@ -76,8 +76,8 @@ struct TraceArgs {
   uint32_t min_votes;          // lanes that must want a treelet before a warp stages it
   const uint32_t* hint;        // staged: predicted next treelet per (treelet, direction octant), or null
   uint32_t wait_tries;         // staged: probes of the wait for the pinned image before staging stops
-  uint32_t tbuf_off;           // byte offset of the trace staging area in dynamic shared memory
-                               // (128-aligned base), kNone: trace entries go straight to the rows
+  uint32_t tbuf_off;           // plain walk: byte offset of the trace staging area in dynamic shared
+                               // memory (128-aligned base), kNone: trace entries go straight to the rows
   uint32_t ss_off;             // plain walk with SHORT: byte offset of the short stacks, likewise
 };
 
@@ -85,12 +85,11 @@ struct TraceArgs {
 // 4-byte entry at a time leaves partly written 32-byte sectors that L2 fills
 // from DRAM and writes back again and again (4.5x the entries' bytes
 // written, as many read, on bounce rays).  Instead each lane keeps its ray's
-// next 8 entries
-// of each row in its warp's 2 KiB staging area ([visit | treelet][entry
-// 0..7][lane] words: lanes hit distinct banks) and writes them as one whole,
-// aligned sector.  Used when the row capacity is a multiple of 8 and the rows
-// start on 32-byte boundaries; the last partial sector is written when the
-// ray ends.
+// next 8 entries of each row in its warp's 2 KiB staging area ([visit |
+// treelet][entry 0..7][lane] words: lanes hit distinct banks) and writes them
+// as one whole, aligned sector.  Used when the row capacity is a multiple of
+// 8 and the rows start on 32-byte boundaries; the last partial sector is
+// written when the ray ends.
 constexpr uint32_t kTraceBufWarpBytes = 2048;
 
 extern __shared__ __align__(128) uint8_t rt_dyn_smem[];
