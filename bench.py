@@ -394,6 +394,16 @@ def run_gpu(args, rank: int, world: int) -> None:
                 prefix + "primary_mrays_s": n_prim / (sum(msp) / len(msp)) / 1e3,
                 prefix + "bounce_mrays_s": n_prim / (sum(msb) / len(msb)) / 1e3}
 
+    def visits(ms, msp, msb):
+        """Transactions per ray of the last step's launches (the hit records'
+        n_visits) and node visits per second: the walks' per-visit rates,
+        apart from how many visits each traversal order makes."""
+        vp = float(d_hits_p.view(torch.int32).view(-1, 16)[:, 11].double().mean())
+        vb = float(d_hits_b.view(torch.int32).view(-1, 16)[:, 11].double().mean())
+        tp, tb = sum(msp) / len(msp), sum(msb) / len(msb)
+        return {"visits_per_ray_primary": vp, "visits_per_ray_bounce": vb,
+                "primary_gvisits_s": n_prim * vp / tp / 1e6, "bounce_gvisits_s": n_prim * vb / tb / 1e6}
+
     # correctness guard: staged hits must equal treelet-order hits on the full batch
     with torch.cuda.stream(stream):
         scene.trace(d_prim, d_hits_p, rt.MODE_TREELET, stream=sp, n=n_prim)
@@ -407,7 +417,9 @@ def run_gpu(args, rank: int, world: int) -> None:
 
     results = {}
     for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET)):
-        results[name] = rates(*timed(mode, max(3, args.steps // 2), args.warmup))
+        t = timed(mode, max(3, args.steps // 2), args.warmup)
+        results[name] = rates(*t)
+        results[name].update(visits(*t))
 
     # headline: staged, with clocks sampled during the timed region
     if dist:
@@ -431,6 +443,7 @@ def run_gpu(args, rank: int, world: int) -> None:
         t_local = float(t.item())
     value = n_rays * args.steps * world / t_local / 1e6
     results["staged"] = rates(ms, msp, msb)
+    results["staged"].update(visits(ms, msp, msb))
 
     # traced timings: every mode writing its visit and treelet-id rows
     for name, mode in (("plain", rt.MODE_PLAIN), ("treelet", rt.MODE_TREELET), ("staged", rt.MODE_STAGED)):
