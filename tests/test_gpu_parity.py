@@ -573,3 +573,29 @@ def test_packed_host_traces_chunked(ctx, mapped):
         st = scene.stats()
         assert st["node_bytes"] == ref_stats["node_bytes"] and st["device_status"] == 0, name
     scene.close()
+
+
+def test_pinned_images_kept_across_tuning_switches(ctx):
+    """Switching pinned_bytes back and forth (as a caller tuning primary and
+    bounce batches separately does) takes the image kept for each budget
+    instead of rebuilding it; the images and the hits stay those of each
+    budget."""
+    import treelet_rt as rt
+    from oracle import oracle as orc
+
+    blob = rt.Blob.gen(rt.SCENE_CUBE_PLANE, 65536, 14)
+    rays = rt.camera_rays(rt.default_camera(rt.SCENE_CUBE_PLANE), 64, 64, 1, 6, 1e-4, 1e30)
+    scene = rt.Scene(ctx, blob)
+    scene.form_treelets(8192)
+    oh, _, _ = orc.trace(blob.bytes(), rays, 1, orc.Treelets(blob.bytes(), 8192), threads=8)
+    seen = {}
+    for budget in (1024, 4096, 1024, 16384, 4096, 1024):
+        scene.set_tuning(pinned_bytes=budget)
+        info = scene.pinned_info()
+        assert 0 < info["bytes"] <= budget
+        if budget in seen:
+            assert info == seen[budget], f"budget {budget}: a different image after switching back"
+        seen[budget] = info
+        hits, _, _ = scene.trace_host(rays, rt.MODE_STAGED)
+        assert_hits_equal(hits, oh, f"staged hits at pinned budget {budget}")
+    scene.close()

@@ -132,6 +132,17 @@ struct rt_scene {
   uint8_t* d_pin = nullptr;
   rt_pinned_info pin_info{0, 0, 0, 0};
   uint32_t pin_root = 0;
+  uint32_t pin_want = 0;  // the pinned_bytes the current image was built for
+  // Images built for other pinned_bytes values under the current partition,
+  // route bits and pin order, so that switching the tuning back and forth
+  // (e.g. per ray batch) does not rebuild and re-upload them.
+  struct PinImage {
+    uint32_t want;
+    uint8_t* d;
+    rt_pinned_info info;
+    uint32_t root;
+  };
+  std::vector<PinImage> pin_cache;
   // per-launch counters and status (library scratch)
   unsigned long long* d_stats = nullptr;
   uint32_t* d_status = nullptr;
@@ -183,10 +194,13 @@ void free_treelets(rt_scene* s) {
   cudaFree(s->d_hint);
   cudaFree(s->d_route);
   cudaFree(s->d_pin);
+  for (auto& im : s->pin_cache) cudaFree(im.d);
+  s->pin_cache.clear();
   s->d_route = nullptr;
   s->d_pin = nullptr;
   s->pin_info = rt_pinned_info{0, 0, 0, 0};
   s->pin_root = 0;
+  s->pin_want = 0;
   s->route.clear();
   s->pin_default.clear();
   s->pin_order.clear();
@@ -236,6 +250,28 @@ uint32_t persistent_grid(const void* kern, uint32_t threads, uint32_t n, size_t 
   return (uint32_t)std::max<uint64_t>(1, std::min(full, need));
 }
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`, once
+// per (device, kernel, limit): a launch whose tuning switches between
+// budgets (pinned images of different sizes per ray batch) then makes no
+// attribute call at all once the largest has been set.
+cudaError_t ensure_dyn_smem(const void* kern, size_t bytes) {
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<int, const void*>, size_t>> set;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto& kv : set) {
+    if (kv.first.first != dev || kv.first.second != kern) continue;
+    if (kv.second >= bytes) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) kv.second = bytes;
+    return e;
+  }
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) set.push_back({{dev, kern}, bytes});
+  return e;
+}
+
 int max_smem_per_block() {
   int dev = 0, v = 0;
   cudaGetDevice(&dev);
@@ -249,7 +285,14 @@ uint32_t staged_smem_limit() {
   return v > 0 ? (uint32_t)v : 0u;
 }
 
-rt_status rebuild_pinned(rt_scene* s);
+rt_status rebuild_pinned(rt_scene* s, bool keep_current = false);
+
+// Frees the images kept for other pinned_bytes values (their partition,
+// route bits or order changed).
+void drop_pin_cache(rt_scene* s) {
+  for (auto& im : s->pin_cache) cudaFree(im.d);
+  s->pin_cache.clear();
+}
 
 // Computes the route bits of the walk (treelets.h) into s->route, uploads
 // them and rebuilds the pinned image that embeds them.  With a nonzero
@@ -265,18 +308,40 @@ rt_status upload_route(rt_scene* s) {
   if (s->offset_quirk)
     for (uint16_t& r : s->route) r &= (uint16_t)~((0x3Fu << rtt::kRouteOtherShift) | (2u << rtt::kRouteInstShift));
   RT_CUDA(cudaMemcpy(s->d_route, s->route.data(), sizeof(uint16_t) * s->route.size(), cudaMemcpyHostToDevice));
+  drop_pin_cache(s);
   return rebuild_pinned(s);
 }
 
 // Rebuilds the pinned image for the scene's order and budget (the budget is
-// clamped to what a CTA can hold).
-rt_status rebuild_pinned(rt_scene* s) {
-  cudaFree(s->d_pin);
+// clamped to what a CTA can hold).  keep_current (a tuning change) keeps the
+// image being replaced for a later switch back, and takes a kept image for
+// the new budget instead of building it again.
+rt_status rebuild_pinned(rt_scene* s, bool keep_current) {
+  constexpr size_t kPinCache = 4;
+  if (keep_current && s->d_pin) {
+    if (s->pin_cache.size() == kPinCache) {
+      cudaFree(s->pin_cache.front().d);
+      s->pin_cache.erase(s->pin_cache.begin());
+    }
+    s->pin_cache.push_back({s->pin_want, s->d_pin, s->pin_info, s->pin_root});
+  } else {
+    cudaFree(s->d_pin);
+  }
   s->d_pin = nullptr;
   s->pin_info = rt_pinned_info{0, 0, 0, 0};
   s->pin_root = 0;
+  s->pin_want = 0;
   const uint32_t want = s->tuning.pinned_bytes;
   if (!s->has_treelets || want == RT_TUNING_OFF || want == 0) return RT_OK;
+  for (size_t i = 0; i < s->pin_cache.size(); ++i) {
+    if (s->pin_cache[i].want != want) continue;
+    s->d_pin = s->pin_cache[i].d;
+    s->pin_info = s->pin_cache[i].info;
+    s->pin_root = s->pin_cache[i].root;
+    s->pin_want = want;
+    s->pin_cache.erase(s->pin_cache.begin() + (ptrdiff_t)i);
+    return RT_OK;
+  }
   const uint32_t budget = std::min(want, staged_smem_limit() > 128 ? staged_smem_limit() - 128 : 0u);
   if (s->pin_default.empty() && s->pin_order.empty())
     rtt::default_pin_order(s->host_blob.data(), s->blob_bytes, s->pin_default, s->part);
@@ -289,6 +354,7 @@ rt_status rebuild_pinned(rt_scene* s) {
   RT_CUDA(cudaMemcpy(s->d_pin, pin.bytes.data(), pin.bytes.size(), cudaMemcpyHostToDevice));
   s->pin_info = rt_pinned_info{(uint32_t)pin.bytes.size(), pin.n_treelets, pin.n_records, pin.root_soff ? 1u : 0u};
   s->pin_root = pin.root_soff;
+  s->pin_want = want;
   return RT_OK;
 }
 
@@ -377,8 +443,8 @@ rt_status launch_queued(rtk::TraceArgs& a, const rt_tuning& t, uint32_t largest_
   const size_t dyn = (size_t)(bt / 32) * slot + 128;
   auto kern = rtk::trace_queued_kernel<CAP, false>;
   auto fin = rtk::trace_queued_kernel<CAP, true>;
-  RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-  RT_CUDA(cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, 128));
+  RT_CUDA(ensure_dyn_smem((const void*)kern, dyn));
+  RT_CUDA(ensure_dyn_smem((const void*)fin, 128));
   const uint32_t grid = persistent_grid((const void*)kern, bt, a.n, dyn);
   const uint32_t grid_fin = persistent_grid((const void*)fin, bt, a.n, 128);
   a.min_votes = t.staged_min_votes;
@@ -490,7 +556,7 @@ rt_status launch_cap(rtk::TraceArgs& a, uint32_t mode, const rt_tuning& t, uint3
     const size_t dyn = (size_t)a.pin_bytes + (size_t)warps * slots * slot_bytes + 128;
     auto kern = slots ? (traced ? rtk::trace_staged_kernel<CAP, true, true> : rtk::trace_staged_kernel<CAP, true, false>)
                       : (traced ? rtk::trace_staged_kernel<CAP, false, true> : rtk::trace_staged_kernel<CAP, false, false>);
-    RT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+    RT_CUDA(ensure_dyn_smem((const void*)kern, dyn));
     kern<<<persistent_grid((const void*)kern, bt, a.n, dyn), bt, dyn, st>>>(a);
   }
   RT_CUDA(cudaGetLastError());
@@ -749,7 +815,7 @@ rt_status rt_scene_set_tuning(rt_scene* s, const rt_tuning* t) {
   s->tuning = n;
   if (repin && s->has_treelets) {
     RT_CUDA(cudaSetDevice(s->ctx->device));
-    return rebuild_pinned(s);
+    return rebuild_pinned(s, true);
   }
   return RT_OK;
 }
@@ -761,6 +827,7 @@ rt_status rt_scene_set_pin_order(rt_scene* s, const uint32_t* order, uint32_t n)
   if (order) s->pin_order.assign(order, order + n);
   else s->pin_order.clear();
   RT_CUDA(cudaSetDevice(s->ctx->device));
+  drop_pin_cache(s);
   return rebuild_pinned(s);
 }
 

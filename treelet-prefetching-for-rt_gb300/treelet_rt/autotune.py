@@ -27,7 +27,7 @@ OFF = 0xFFFFFFFF  # RT_TUNING_OFF
 GRID_STAGED = {
     "staged_threads": [64, 128, 256],
     "refill_lanes": [4, 8, 16, 32],
-    "pinned_bytes": [OFF, 4096, 16384, 65536],
+    "pinned_bytes": [OFF, 1024, 2048, 4096, 16384, 65536],
     "staged_slots": [OFF, 1, 2, 4],
     "staged_slot_bytes": [1024, 2048, 4096, 65536],
     "staged_epoch": [4, 16, 64],
