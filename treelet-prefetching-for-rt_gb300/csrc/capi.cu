@@ -1553,8 +1553,7 @@ __global__ void trace_offsets_kernel(uint32_t* __restrict__ off, const uint32_t*
 
 // One warp per ray: the ray's global offset (base + chunk offset) into
 // `goff`, and the used prefix of its trace rows to its place in the packed
-// arrays (NULL: not written).  Destinations may be device memory or mapped,
-// page-locked host memory.
+// staging arrays (NULL: not written).
 __global__ void trace_pack_kernel(const uint32_t* __restrict__ vis_rows, const uint32_t* __restrict__ tl_rows,
                                   const uint32_t* __restrict__ off, uint32_t n, uint32_t cap, uint32_t chunk_total,
                                   unsigned long long base, unsigned long long* __restrict__ goff,
@@ -1575,11 +1574,11 @@ __global__ void trace_pack_kernel(const uint32_t* __restrict__ vis_rows, const u
 
 }  // namespace
 
-// Chunks pipeline the call: rays of every chunk go in on one stream; chunk c
-// is traced, counted and scanned on one of two streams while the host waits
-// for chunk c-1's total, then packs chunk c-1 into a device staging area and
-// copies it out on a third, so that copies and packing overlap the next
-// chunk's trace.
+// Chunks pipeline the call: the rays of every chunk go in on one stream;
+// each chunk is traced, counted and scanned on one of two streams; the host
+// waits for chunk c's total, queues its packing (into a device staging area)
+// and copies on a third stream, and then queues chunk c + 1's trace, so that
+// the copies of chunk c overlap the trace of chunk c + 1.
 extern "C" rt_status rt_trace_host_packed(rt_scene* s, const rt_ray* rays, const uint32_t* flags,
                                           uint32_t default_flags, uint32_t n, uint32_t mode, uint32_t row_capacity,
                                           rt_hit* hits, uint64_t* offsets, uint32_t* visits, uint32_t* treelets,
