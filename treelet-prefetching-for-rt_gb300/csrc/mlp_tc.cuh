@@ -14,13 +14,15 @@
 //   out_dh2_kernel    per (row tile, column split): dz for the tile, then
 //                     dh2 += dz . W3 on the tensor cores, summed across
 //                     splits with atomics;
-//   out_dw3_kernel    per 256-column chunk: over every row tile, dz^T, then
-//                     [dW3 | db3]^T += dz^T . [h2 | 1] on the tensor cores.
+//   out_dw3_kernel    per 128-column chunk and half of the row tiles: dz^T,
+//                     then [dW3 | db3]^T += dz^T . [h2 | 1] on the tensor
+//                     cores, added into the zeroed gradient.
 //
 // Operands live in shared memory in the canonical K-major layout without
 // swizzle: 8-row x 16-byte core matrices, core matrices of one row group
-// 128 bytes apart along K (the leading-dimension offset), row groups
-// 16 * (K extent) bytes apart (the stride-dimension offset).  One thread issues
+// 128 bytes apart along K (the leading-dimension offset; 144 in the dW3
+// pass's dz^T tile), row groups 16 * (K extent) bytes apart (the
+// stride-dimension offset).  One thread issues
 // the MMAs and commits them to an mbarrier; every wait is bounded and a wait
 // that gives up sets the status word instead of hanging.
 #pragma once
